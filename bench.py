@@ -1,0 +1,342 @@
+"""Benchmark: Fr NTT throughput at 2^24 on GB300 (plus the other operators).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one forward NTT of 2^24 seeded random canonical Fr elements
+(512 MiB, larger than the 129 MB L2, so no flush is needed between steps).
+`value` is device throughput with the input resident in HBM (Melem/s =
+2^24 * K * n_gpus / max-over-ranks time); `e2e` is the same metric through the
+C ABI with host buffers: each step copies the input from pinned host memory,
+transforms it and copies the result back.  `roofline` is the integer-multiply
+pipe bound of the transform kernel; `roofline_hbm` its HBM view.  Extra
+operators (INTT, LDE, grand products, evaluation, division) are timed after
+the headline and reported under `ops`.
+
+--impl reference times the reference's CPU path for the same workload on the
+host cores (the oracle's restatement: the reference has no CPU NTT of its own)
+and prints the same metric with "impl": "reference".
+Under torchrun with N > 1 each rank transforms its own polynomial on its own
+GPU (replicas; there is no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LG_N = 24
+N = 1 << LG_N
+MM_PER_NTT = (N // 2) * LG_N          # algorithmic Montgomery multiplies (radix-2 count)
+INSTR_PER_MM = 256                     # 8x8 limbs: 4 n^2 integer multiply instructions
+BYTES_PER_NTT = 2 * 32 * N             # read + write once
+IMAD_PER_CLK_PER_SM = 64               # 32-bit multiply-add lanes per SM per clock (measured)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-ops", action="store_true", help="skip the secondary operator timings")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch recorded from an ncu capture (profiles/<name>)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def time_device(fn, steps, warmup, torch):
+    """CUDA-event time of `steps` calls of fn() on the current stream (ms total)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def cpu_ntt_rate(lg: int, reps: int, threads: int):
+    from oracle import oracle as O
+
+    x = O.random_fr(1 << lg, 0x5EED0018)
+    O.ntt(x[:1024].copy(), nthreads=threads)  # load / warm the library
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.ntt(x, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return (1 << lg) * reps / dt / 1e6, dt
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    reps = max(1, args.steps // 10)
+    for _ in range(min(args.warmup, 1)):
+        cpu_ntt_rate(20, 1, threads)
+    rate, dt = cpu_ntt_rate(LG_N, reps, threads)
+    line = {
+        "impl": "reference", "metric": "fr_ntt_2^24_throughput", "value": round(rate, 3),
+        "unit": "Melem/s", "n_gpus": args.gpus, "steps": reps, "warmup": args.warmup,
+        "ms_per_step": round(dt / reps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32x8 (Fr, Montgomery)", "data": "synthetic (seeded SplitMix64 Fr)",
+        "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N},
+        "cpu_baseline": {"value": round(rate, 3), "unit": "Melem/s", "cores": threads, "kind": "port",
+                         "sample": "%d full 2^24 NTTs (oracle restatement; the reference has no CPU NTT)" % reps},
+        "e2e": {"value": round(rate, 3), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+
+    pp = ge.load_package()
+    ppfr = pp.ppfr
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = dist_mod
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # ---- device-resident headline
+    x = pp.random_fr(N, 0x5EED0018 + rank)
+    out = ppfr.empty(N)
+    ppfr.prepare(LG_N, False)
+    fn = lambda: pp.ntt(x, out=out)  # noqa: E731
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = pp.launch_count()
+    torch.cuda.synchronize()
+    barrier()
+    ms = time_device(fn, args.steps, 0, torch)
+    launches = pp.launch_count() - launches0
+    torch.cuda.synchronize()
+    barrier()
+    # ---- end to end through the C ABI with host buffers
+    hin = torch.empty((N, 4), dtype=torch.int64, pin_memory=True)
+    hin.copy_(x.cpu())
+    hout = torch.empty_like(hin, pin_memory=True)
+    dbuf = ppfr.empty(N)
+
+    def e2e_step():
+        dbuf.copy_(hin, non_blocking=True)
+        pp.ntt(dbuf, out=dbuf)
+        hout.copy_(dbuf, non_blocking=True)
+
+    e2e_steps = max(3, args.steps // 2)
+    e2e_ms = time_device(e2e_step, e2e_steps, 1, torch)
+    clk = clocks.stop()
+    # max over ranks
+    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms, e2e_ms_norm = float(t[0]), float(t[1])
+    value = N * args.steps * world / (ms / 1e3) / 1e6
+    e2e_value = N * args.steps * world / (e2e_ms_norm / 1e3) / 1e6
+
+    ops = {}
+    if not args.no_ops and rank == 0:
+        ops = secondary_ops(pp, torch)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks, peak_kind = load_peaks()
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    int_peak = n_sm * IMAD_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12  # T instr / s
+    sec_per_ntt = ms / args.steps / 1e3
+    achieved_int = MM_PER_NTT * INSTR_PER_MM / sec_per_ntt / 1e12
+    achieved_hbm = BYTES_PER_NTT / sec_per_ntt / 1e9
+    # one NTT is len(split) kernel launches; per-launch figures are the same ratio
+    traffic = profile_traffic("ntt_pass_2p24_traffic.txt")
+    cpu_rate, cpu_dt = cpu_ntt_rate(LG_N, 2, os.cpu_count() or 1)
+    line = {
+        "metric": "fr_ntt_2^24_throughput", "value": round(value, 3), "unit": "Melem/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32x8 (Fr, Montgomery)", "data": "synthetic (seeded SplitMix64 Fr)",
+        "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N,
+                   "l2_flush": "not needed: 512 MiB input > 129 MB L2", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Melem/s", "h2d_bytes_per_step": 32 * N,
+                "d2h_bytes_per_step": 32 * N},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "int", "kernel": "k_ntt_pass", "achieved": round(achieved_int, 3),
+                     "peak": round(int_peak, 3), "unit": "Tinstr/s", "frac": round(achieved_int / int_peak, 4),
+                     "traffic": traffic,
+                     "note": "algorithmic (N/2)lgN Montgomery multiplies x 256 32-bit multiply instructions; "
+                             "peak = SMs x 64 multiply lanes/clk x median SM clock under load"},
+        "roofline_hbm": {"bound": "hbm", "achieved": round(achieved_hbm, 2), "peak": peaks.get("hbm_gbs"),
+                         "unit": "GB/s", "frac": round(achieved_hbm / peaks.get("hbm_gbs", 6800.0), 4),
+                         "peak_kind": peak_kind},
+        "cpu_baseline": {"value": round(cpu_rate, 3), "unit": "Melem/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": "2 full 2^24 NTTs of the oracle restatement, all host threads"},
+        "clocks": clk,
+        "ops": ops,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def secondary_ops(pp, torch):
+    """Quick device timings of the other operators (inputs resident)."""
+    import numpy as np
+
+    ppfr = pp.ppfr
+    res = {}
+
+    def rate(name, fn, elems, reps=5):
+        ms = time_device(fn, reps, 2, torch)
+        res[name] = {"ms": round(ms / reps, 4), "Melem_per_s": round(elems * reps / (ms / 1e3) / 1e6, 2)}
+
+    for lg in (22, 26):
+        x = pp.random_fr(1 << lg, lg)
+        o = ppfr.empty(1 << lg)
+        rate("ntt_2^%d" % lg, lambda: pp.ntt(x, out=o), 1 << lg, 3)
+        del x, o
+    x = pp.random_fr(N, 1)
+    o = ppfr.empty(N)
+    rate("intt_2^24", lambda: pp.ntt(x, True, out=o), N)
+    del o
+    for lam in (2, 3):
+        o = ppfr.empty(N << lam)
+        rate("lde_coeffs_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_COEFFS, out=o), N, 3)
+        rate("lde_evals_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_EVALS, out=o), N, 3)
+        del o
+    del x
+    n = 1 << 20
+    p = pp.random_fr(n, 2)
+    z = pp.random_fr(1, 3)
+    y = ppfr.empty(1)
+    rate("gp_prefix_2^20", lambda: pp.gp_prefix_(p), n, 10)
+    rate("eval_2^20", lambda: pp.evaluate(p, z, out=y), n, 10)
+    rate("div_2^20", lambda: pp.div_xplusc_(p, z), n, 10)
+    w = [pp.random_fr(n, 10 + j) for j in range(3)]
+    s = [pp.random_fr(n, 20 + j) for j in range(3)]
+    params = pp.random_fr(5, 30)
+    zz = ppfr.empty(n)
+    rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
+    return res
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

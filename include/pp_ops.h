@@ -1,0 +1,115 @@
+/*
+ * pp_ops.h -- C ABI of the GB300 Fr prover-operator library (libppfr.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Field elements are
+ * BLS12-381 scalar-field values, 32 bytes each: 4 little-endian uint64 limbs,
+ * Montgomery form with R = 2^256, canonical (< r) -- the reference's in-memory
+ * format (PLONK/utils/mont/cuda/ff/bls12-381.hpp:7-45; raw files read by
+ * miss_ops.cu:8-24).  "d_" pointers are device pointers of the current CUDA
+ * device; "stream" is a cudaStream_t (NULL = legacy default stream).  All
+ * calls are stream-ordered and asynchronous unless stated otherwise; the
+ * caller owns all buffers.  The library owns only cached constant tables and
+ * per-stream workspace, created on first use and kept until pp_release().
+ *
+ * Every call returns PP_OK (0) or an error status; it never exits or traps.
+ * pp_last_error() gives a message for the calling thread's last failure.
+ */
+#ifndef PP_OPS_H
+#define PP_OPS_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PP_OK 0
+#define PP_E_INVAL 1       /* bad argument (size, alignment, null pointer) */
+#define PP_E_NOMEM 2       /* device allocation failed or over the memory budget */
+#define PP_E_CUDA 3        /* CUDA runtime error */
+#define PP_E_TIMEOUT 4     /* a bounded device-side wait ran out */
+#define PP_E_UNSUPPORTED 5 /* size outside what this build supports */
+#define PP_E_CANCELLED 6   /* serving: request cancelled */
+#define PP_E_BUSY 7        /* serving: admission refused (queue or budget full) */
+
+#define PP_MAX_LG_N 30 /* largest transform handled: 2^30 elements */
+
+const char *pp_status_string(int status);
+const char *pp_last_error(void);
+/* library version string and build architecture ("sm_103a") */
+const char *pp_version(void);
+
+/* ---------------------------------------------------------------- NTT ---
+ * Natural-order in, natural-order out transform of 2^lg_n elements,
+ * X_k = sum_j x_j w^(jk) with w = 7^((r-1)/2^lg_n); inverse = 1 uses w^-1 and
+ * scales by 2^-lg_n.  d_in == d_out is allowed (in place).
+ * Replaces Ntt::forward / Intt::forward (PLONK/utils/function.cu:280, :330 ->
+ * PLONK/utils/zkp/cuda/zksnark_ntt.cu:342-393), the transform the reference's
+ * segmented our_ntt (ntt.cu:979-1037) and four-step standard4_ntt
+ * (ntt.cu:1039-1138) reproduce bit for bit.  0 <= lg_n <= PP_MAX_LG_N. */
+int pp_ntt(const void *d_in, void *d_out, uint32_t lg_n, int inverse, void *stream);
+
+/* ---------------------------------------------------------------- LDE ---
+ * Low-degree extension onto 2^(lg_n+lambda) points, natural order out.
+ *  mode 0 (PP_LDE_COEFFS): d_in holds 2^lg_n coefficients a_i; output is
+ *    p(h * w_L^k) with h = 7^(2^lambda), w_L the 2^(lg_n+lambda)-th root:
+ *    the function the reference's our_lde computes (lde.cu:1267-1365 with
+ *    lde_spread_powers_kernel lde.cu:623-648).
+ *  mode 1 (PP_LDE_EVALS): d_in holds evaluations on the size-2^lg_n subgroup;
+ *    INTT, multiply coefficient i by 7^i, zero-pad, NTT: p(7 * w_L^k).
+ *  mode 2 (PP_LDE_SPREAD): the reference's naive_lde baseline (lde.cu:1367,
+ *    spread at :479-491): inputs placed at i << lambda, no coset factor.
+ * d_out must not overlap d_in.  lambda <= 8. */
+#define PP_LDE_COEFFS 0
+#define PP_LDE_EVALS 1
+#define PP_LDE_SPREAD 2
+int pp_lde(const void *d_in, void *d_out, uint32_t lg_n, uint32_t lambda, uint32_t mode,
+           void *stream);
+
+/* ------------------------------------------------------- grand product ---
+ * Exclusive prefix product in place: out[0] = 1, out[i] = prod_{j<i} in[j].
+ * Replaces accumulate_mul_poly (PLONK/utils/function.cu:256 ->
+ * PLONK/utils/mont/cuda/mont_arithmetic.cu:334-361, :544-550). n >= 1. */
+int pp_gp_prefix(void *d_inout, uint64_t n, void *stream);
+
+/* PLONK copy-constraint grand product over 2^lg_n rows:
+ *   ratio_i = prod_j (w_j[i] + beta*k_j*w^i + gamma) / prod_j (w_j[i] + beta*sigma_j[i] + gamma)
+ *   z = exclusive prefix product of ratio (z_0 = 1)
+ * d_w / d_sigma: 3 device pointers each; d_params: device array of 5 elements
+ * (beta, gamma, k1, k2, k3).  A zero denominator contributes a factor 0.
+ * The reference's permutation-constraint kernel uses this ratio form
+ * (PLONK/utils/zkp/cuda/zksnark_compute_permutation_constraint.cu:13-34) and
+ * passes its product to accumulate_mul_poly. */
+int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, const void *d_params, void *d_z,
+               uint32_t lg_n, void *stream);
+
+/* --------------------------------------------------------- evaluation ---
+ * d_y[0] = sum_i poly[i] * x^i (x = d_x[0]); n == 0 gives 0.
+ * Replaces evaluate (PLONK/utils/function.cu:170-181 ->
+ * mont_arithmetic.cu:104-163, :507-529). */
+int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_y, void *stream);
+
+/* ----------------------------------------------------------- division ---
+ * In place: the buffer p (n coefficients) becomes q with q_i = S_{i+1},
+ * S_i = sum_{j>=i} p_j (-c)^(j-i), q_{n-1} = 0 -- the quotient of p by (X + c)
+ * (equivalently of (p(X) - p(z)) by (X - z), z = -c).
+ * Replaces poly_div_poly (PLONK/utils/function.cu:183 ->
+ * mont_arithmetic.cu:305-331, :531-542).  n >= 1. */
+int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *stream);
+
+/* ----------------------------------------------------------- utilities --- */
+/* n seeded uniformly random canonical elements: element (first_index + i)
+ * limb j is the SplitMix64 output at counter ((first_index+i) << 8 | t << 2 | j)
+ * of the stream seeded with seed, bit 255 cleared, rejection-sampled < r
+ * (attempt t), stored as the Montgomery representation. */
+int pp_random_fr(void *d_out, uint64_t n, uint64_t seed, uint64_t first_index, void *stream);
+
+/* number of kernel launches this library has issued from the calling process */
+uint64_t pp_launch_count(void);
+
+/* drop cached tables and workspaces of the current device (synchronises it) */
+int pp_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,445 @@
+// fr.cuh -- BLS12-381 scalar field Fr on 8 x 32-bit limbs, Montgomery form.
+//
+// Storage is the reference's: 4 little-endian uint64 limbs (= 8 little-endian
+// uint32 limbs), Montgomery representation with R = 2^256, canonical (< r)
+// (PLONK/utils/mont/cuda/ff/bls12-381.hpp:7-45, mont_t.cuh:34).
+//
+// Arithmetic is written once over "carry-chain primitives" that map 1:1 onto
+// PTX integer instructions with the condition-code carry (add.cc, addc,
+// mad.lo.cc, madc.hi ...).  On the device they are inline PTX; on the host the
+// same functions emulate the carry flag exactly, so every multiply variant is
+// unit-tested on the CPU against the oracle before it runs on a GPU.
+//
+// Multiplication is Montgomery CIOS (Koc, Acar, Kaliski, "Analyzing and
+// comparing Montgomery multiplication algorithms", IEEE Micro 1996) on 32-bit
+// words.  r = 1 (mod 2^32) gives -r^-1 = 0xffffffff, so each row's m is a
+// negation, and the two lowest words of r (1 and 0xffffffff) make m*r[0] and
+// m*r[1] multiply-free: each row costs 16 + 12 integer multiplies instead of
+// 16 + 16.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PP_HD __host__ __device__ __forceinline__
+#else
+#define PP_HD inline
+#endif
+
+namespace pp {
+
+// r, 32-bit limbs, least significant first
+#define PP_R0 0x00000001u
+#define PP_R1 0xffffffffu
+#define PP_R2 0xfffe5bfeu
+#define PP_R3 0x53bda402u
+#define PP_R4 0x09a1d805u
+#define PP_R5 0x3339d808u
+#define PP_R6 0x299d7d48u
+#define PP_R7 0x73eda753u
+
+struct fr {
+  uint32_t v[8];
+};
+
+// ---------------------------------------------------------------------------
+// carry-chain primitives
+// ---------------------------------------------------------------------------
+#if !defined(__CUDA_ARCH__)
+inline uint32_t &host_cf() {
+  static thread_local uint32_t cf = 0;
+  return cf;
+}
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define PP_ASM1(op, a, b)                                                     \
+  uint32_t r;                                                                 \
+  asm volatile(op " %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));                 \
+  return r
+#define PP_ASM2(op, a, b, c)                                                  \
+  uint32_t r;                                                                 \
+  asm volatile(op " %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));     \
+  return r
+#endif
+
+PP_HD uint32_t add_cc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("add.cc.u32", a, b);
+#else
+  uint64_t s = (uint64_t)a + b;
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t addc_cc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("addc.cc.u32", a, b);
+#else
+  uint64_t s = (uint64_t)a + b + host_cf();
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t addc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("addc.u32", a, b);
+#else
+  return (uint32_t)((uint64_t)a + b + host_cf());
+#endif
+}
+PP_HD uint32_t sub_cc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("sub.cc.u32", a, b);
+#else
+  host_cf() = a < b;
+  return a - b;
+#endif
+}
+PP_HD uint32_t subc_cc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("subc.cc.u32", a, b);
+#else
+  uint64_t bb = (uint64_t)b + host_cf();
+  host_cf() = (uint64_t)a < bb;
+  return (uint32_t)((uint64_t)a - bb);
+#endif
+}
+PP_HD uint32_t subc(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM1("subc.u32", a, b);
+#else
+  return (uint32_t)((uint64_t)a - b - host_cf());
+#endif
+}
+PP_HD uint32_t mullo(uint32_t a, uint32_t b) { return a * b; }
+PP_HD uint32_t mulhi(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+PP_HD uint32_t madlo_cc(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("mad.lo.cc.u32", a, b, c);
+#else
+  uint64_t s = (uint64_t)(uint32_t)(a * b) + c;
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t madloc_cc(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("madc.lo.cc.u32", a, b, c);
+#else
+  uint64_t s = (uint64_t)(uint32_t)(a * b) + c + host_cf();
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t madloc(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("madc.lo.u32", a, b, c);
+#else
+  return (uint32_t)((uint64_t)(uint32_t)(a * b) + c + host_cf());
+#endif
+}
+PP_HD uint32_t madhi_cc(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("mad.hi.cc.u32", a, b, c);
+#else
+  uint64_t s = (((uint64_t)a * b) >> 32) + c;
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t madhic_cc(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("madc.hi.cc.u32", a, b, c);
+#else
+  uint64_t s = (((uint64_t)a * b) >> 32) + c + host_cf();
+  host_cf() = (uint32_t)(s >> 32);
+  return (uint32_t)s;
+#endif
+}
+PP_HD uint32_t madhic(uint32_t a, uint32_t b, uint32_t c) {
+#if defined(__CUDA_ARCH__)
+  PP_ASM2("madc.hi.u32", a, b, c);
+#else
+  return (uint32_t)((((uint64_t)a * b) >> 32) + c + host_cf());
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// constants
+// ---------------------------------------------------------------------------
+PP_HD fr fr_zero() { return fr{{0, 0, 0, 0, 0, 0, 0, 0}}; }
+// R mod r (Montgomery one)
+PP_HD fr fr_one() {
+  return fr{{0xfffffffeu, 0x00000001u, 0x00034802u, 0x5884b7fau, 0xecbc4ff5u, 0x998c4fefu,
+             0xacc5056fu, 0x1824b159u}};
+}
+// R^2 mod r
+PP_HD fr fr_rr() {
+  return fr{{0xf3f29c6du, 0xc999e990u, 0x87925c23u, 0x2b6cedcbu, 0x7254398fu, 0x05d31496u,
+             0x9f59ff11u, 0x0748d9d9u}};
+}
+
+PP_HD bool fr_is_zero(const fr &a) {
+  return (a.v[0] | a.v[1] | a.v[2] | a.v[3] | a.v[4] | a.v[5] | a.v[6] | a.v[7]) == 0;
+}
+PP_HD bool fr_eq(const fr &a, const fr &b) {
+  uint32_t d = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) d |= a.v[i] ^ b.v[i];
+  return d == 0;
+}
+
+// x - r if x >= r else x, for x < 2^256 (x < 2r)
+PP_HD void fr_reduce_once(uint32_t x[8]) {
+  uint32_t t[8];
+  t[0] = sub_cc(x[0], PP_R0);
+  t[1] = subc_cc(x[1], PP_R1);
+  t[2] = subc_cc(x[2], PP_R2);
+  t[3] = subc_cc(x[3], PP_R3);
+  t[4] = subc_cc(x[4], PP_R4);
+  t[5] = subc_cc(x[5], PP_R5);
+  t[6] = subc_cc(x[6], PP_R6);
+  t[7] = subc_cc(x[7], PP_R7);
+  uint32_t borrow = subc(0, 0);  // 0xffffffff if x < r
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = borrow ? x[i] : t[i];
+}
+
+PP_HD fr fr_add(const fr &a, const fr &b) {
+  fr s;
+  s.v[0] = add_cc(a.v[0], b.v[0]);
+  s.v[1] = addc_cc(a.v[1], b.v[1]);
+  s.v[2] = addc_cc(a.v[2], b.v[2]);
+  s.v[3] = addc_cc(a.v[3], b.v[3]);
+  s.v[4] = addc_cc(a.v[4], b.v[4]);
+  s.v[5] = addc_cc(a.v[5], b.v[5]);
+  s.v[6] = addc_cc(a.v[6], b.v[6]);
+  s.v[7] = addc(a.v[7], b.v[7]);  // a + b < 2r < 2^256
+  fr_reduce_once(s.v);
+  return s;
+}
+
+PP_HD fr fr_sub(const fr &a, const fr &b) {
+  fr d;
+  d.v[0] = sub_cc(a.v[0], b.v[0]);
+  d.v[1] = subc_cc(a.v[1], b.v[1]);
+  d.v[2] = subc_cc(a.v[2], b.v[2]);
+  d.v[3] = subc_cc(a.v[3], b.v[3]);
+  d.v[4] = subc_cc(a.v[4], b.v[4]);
+  d.v[5] = subc_cc(a.v[5], b.v[5]);
+  d.v[6] = subc_cc(a.v[6], b.v[6]);
+  d.v[7] = subc_cc(a.v[7], b.v[7]);
+  uint32_t mask = subc(0, 0);  // all ones on borrow
+  d.v[0] = add_cc(d.v[0], PP_R0 & mask);
+  d.v[1] = addc_cc(d.v[1], PP_R1 & mask);
+  d.v[2] = addc_cc(d.v[2], PP_R2 & mask);
+  d.v[3] = addc_cc(d.v[3], PP_R3 & mask);
+  d.v[4] = addc_cc(d.v[4], PP_R4 & mask);
+  d.v[5] = addc_cc(d.v[5], PP_R5 & mask);
+  d.v[6] = addc_cc(d.v[6], PP_R6 & mask);
+  d.v[7] = addc(d.v[7], PP_R7 & mask);
+  return d;
+}
+
+PP_HD fr fr_neg(const fr &a) { return fr_sub(fr_zero(), a); }
+
+// ---------------------------------------------------------------------------
+// Montgomery multiplication, a * b * 2^-256 mod r
+// ---------------------------------------------------------------------------
+// One CIOS row on the running sum t[0..9] (t[9] receives the top carry):
+// t += ai * b; m = -t[0]; t += m * r; t >>= 32.
+// Variant "s" (special): uses r[0] = 1, r[1] = 2^32 - 1.
+PP_HD void cios_row_s(uint32_t t[10], uint32_t ai, const uint32_t b[8]) {
+  // t[0..8] += lo(ai*b[j]) at j, carry into t[9]
+  t[0] = madlo_cc(ai, b[0], t[0]);
+  t[1] = madloc_cc(ai, b[1], t[1]);
+  t[2] = madloc_cc(ai, b[2], t[2]);
+  t[3] = madloc_cc(ai, b[3], t[3]);
+  t[4] = madloc_cc(ai, b[4], t[4]);
+  t[5] = madloc_cc(ai, b[5], t[5]);
+  t[6] = madloc_cc(ai, b[6], t[6]);
+  t[7] = madloc_cc(ai, b[7], t[7]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(0, 0);
+  // t[1..9] += hi(ai*b[j]) at j+1
+  t[1] = madhi_cc(ai, b[0], t[1]);
+  t[2] = madhic_cc(ai, b[1], t[2]);
+  t[3] = madhic_cc(ai, b[2], t[3]);
+  t[4] = madhic_cc(ai, b[3], t[4]);
+  t[5] = madhic_cc(ai, b[4], t[5]);
+  t[6] = madhic_cc(ai, b[5], t[6]);
+  t[7] = madhic_cc(ai, b[6], t[7]);
+  t[8] = madhic_cc(ai, b[7], t[8]);
+  t[9] = addc(t[9], 0);
+  // m = -t0 (mod 2^32).  m*r[0] + m*r[1]*2^32 = m + (m << 32) - m*... :
+  //   lo(m*1) = m       -> t0 + m == 0 (mod 2^32), carry out = (t0 != 0)
+  //   lo(m*(2^32-1)) = -m = t0,  hi(m*(2^32-1)) = m - (m != 0)
+  const uint32_t t0 = t[0];
+  const uint32_t m = 0u - t0;
+  uint32_t h1;
+  (void)sub_cc(0, m);  // borrow = (m != 0)
+  h1 = subc(m, 0);     // m - (m != 0)
+  (void)add_cc(t0, 0xffffffffu);  // carry = (t0 != 0): the carry out of t0 + m
+  t[1] = addc_cc(t[1], t0);
+  t[2] = madloc_cc(m, PP_R2, t[2]);
+  t[3] = madloc_cc(m, PP_R3, t[3]);
+  t[4] = madloc_cc(m, PP_R4, t[4]);
+  t[5] = madloc_cc(m, PP_R5, t[5]);
+  t[6] = madloc_cc(m, PP_R6, t[6]);
+  t[7] = madloc_cc(m, PP_R7, t[7]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[2] = add_cc(t[2], h1);
+  t[3] = madhic_cc(m, PP_R2, t[3]);
+  t[4] = madhic_cc(m, PP_R3, t[4]);
+  t[5] = madhic_cc(m, PP_R4, t[5]);
+  t[6] = madhic_cc(m, PP_R5, t[6]);
+  t[7] = madhic_cc(m, PP_R6, t[7]);
+  t[8] = madhic_cc(m, PP_R7, t[8]);
+  t[9] = addc(t[9], 0);
+  // shift down one word (t[0] is zero now)
+#pragma unroll
+  for (int k = 0; k < 9; ++k) t[k] = t[k + 1];
+  t[9] = 0;
+}
+
+// Variant "g" (generic CIOS rows, no use of the shape of r).
+PP_HD void cios_row_g(uint32_t t[10], uint32_t ai, const uint32_t b[8]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  t[0] = madlo_cc(ai, b[0], t[0]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j] = madloc_cc(ai, b[j], t[j]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(0, 0);
+  t[1] = madhi_cc(ai, b[0], t[1]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j + 1] = madhic_cc(ai, b[j], t[j + 1]);
+  t[9] = addc(t[9], 0);
+  const uint32_t m = t[0] * 0xffffffffu;
+  t[0] = madlo_cc(m, r[0], t[0]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j] = madloc_cc(m, r[j], t[j]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[1] = madhi_cc(m, r[0], t[1]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j + 1] = madhic_cc(m, r[j], t[j + 1]);
+  t[9] = addc(t[9], 0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) t[k] = t[k + 1];
+  t[9] = 0;
+}
+
+template <int VARIANT>
+PP_HD fr fr_mul_v(const fr &a, const fr &b) {
+  uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (VARIANT == 0)
+      cios_row_s(t, a.v[i], b.v);
+    else
+      cios_row_g(t, a.v[i], b.v);
+  }
+  // t < 2r < 2^256 (t[8] == 0)
+  fr_reduce_once(t);
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[i];
+  return out;
+}
+
+// Variant "w": CIOS in plain C over 64-bit products (compiler-chosen wide
+// multiply-adds), also using r[0] = 1.
+PP_HD fr fr_mul_w(const fr &a, const fr &b) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint64_t c = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      uint64_t s = (uint64_t)a.v[i] * b.v[j] + t[j] + c;
+      t[j] = (uint32_t)s;
+      c = s >> 32;
+    }
+    uint64_t s = (uint64_t)t[8] + c;
+    t[8] = (uint32_t)s;
+    t[9] = (uint32_t)(s >> 32);
+    const uint32_t m = 0u - t[0];
+    c = ((uint64_t)m + t[0]) >> 32;
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+      s = (uint64_t)m * r[j] + t[j] + c;
+      t[j - 1] = (uint32_t)s;
+      c = s >> 32;
+    }
+    s = (uint64_t)t[8] + c;
+    t[7] = (uint32_t)s;
+    t[8] = t[9] + (uint32_t)(s >> 32);
+  }
+  fr_reduce_once(t);
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[i];
+  return out;
+}
+
+#ifndef PP_MUL_VARIANT
+#define PP_MUL_VARIANT 0
+#endif
+
+PP_HD fr fr_mul(const fr &a, const fr &b) {
+#if PP_MUL_VARIANT == 2
+  return fr_mul_w(a, b);
+#else
+  return fr_mul_v<PP_MUL_VARIANT>(a, b);
+#endif
+}
+
+PP_HD fr fr_sqr(const fr &a) { return fr_mul(a, a); }
+
+// a^e for a 64-bit exponent (square and multiply, most significant bit first)
+PP_HD fr fr_pow_u64(const fr &a, uint64_t e) {
+  fr acc = fr_one();
+  bool started = false;
+  for (int bit = 63; bit >= 0; --bit) {
+    if (started) acc = fr_sqr(acc);
+    if ((e >> bit) & 1) {
+      acc = started ? fr_mul(acc, a) : a;
+      started = true;
+    }
+  }
+  return acc;
+}
+
+// a^(r-2) = a^-1 (0 -> 0), Fermat; e = r - 2 as 32-bit limbs, least significant first
+PP_HD fr fr_inv(const fr &a) {
+  const uint32_t e[8] = {0xffffffffu, 0xfffffffeu, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  fr acc = fr_one();
+  // 4-bit fixed window
+  fr tab[16];
+  tab[0] = fr_one();
+  tab[1] = a;
+  for (int i = 2; i < 16; ++i) tab[i] = fr_mul(tab[i - 1], a);
+  for (int w = 7; w >= 0; --w) {
+    for (int nib = 7; nib >= 0; --nib) {
+      if (!(w == 7 && nib == 7)) {
+        acc = fr_sqr(acc);
+        acc = fr_sqr(acc);
+        acc = fr_sqr(acc);
+        acc = fr_sqr(acc);
+      }
+      const uint32_t d = (e[w] >> (4 * nib)) & 15u;
+      acc = fr_mul(acc, tab[d]);
+    }
+  }
+  return acc;
+}
+
+}  // namespace pp

