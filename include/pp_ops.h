@@ -71,6 +71,12 @@ int pp_lde(const void *d_in, void *d_out, uint32_t lg_n, uint32_t lambda, uint32
  * PLONK/utils/mont/cuda/mont_arithmetic.cu:334-361, :544-550). n >= 1. */
 int pp_gp_prefix(void *d_inout, uint64_t n, void *stream);
 
+/* Both scans of the same input: d_excl[i] = prod_{j<i} in[j] and
+ * d_incl[i] = prod_{j<=i} in[j] (either may be NULL or equal d_in).  The
+ * reference's accumulate_mul_poly_(product, output) leaves exactly these in
+ * (product, output) (mont_arithmetic.cu:334-361, :552-556). */
+int pp_gp_scan(const void *d_in, void *d_excl, void *d_incl, uint64_t n, void *stream);
+
 /* PLONK copy-constraint grand product over 2^lg_n rows:
  *   ratio_i = prod_j (w_j[i] + beta*k_j*w^i + gamma) / prod_j (w_j[i] + beta*sigma_j[i] + gamma)
  *   z = exclusive prefix product of ratio (z_0 = 1)

@@ -174,6 +174,15 @@ def fr_inv(a):
     return o
 
 
+def fr_pow(a, e: int) -> np.ndarray:
+    """a^e for an integer exponent 0 <= e < 2^256."""
+    a = _scalar(a)
+    ev = from_int(e)
+    o = np.empty(4, np.uint64)
+    lib().or_fr_pow(a.ctypes.data, ev.ctypes.data, o.ctypes.data)
+    return o
+
+
 def root_of_unity(lg: int, inverse: bool = False) -> np.ndarray:
     o = np.empty(4, np.uint64)
     lib().or_root_of_unity(lg, int(inverse), o.ctypes.data)

@@ -390,13 +390,169 @@ PP_HD fr fr_mul_w(const fr &a, const fr &b) {
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// Karatsuba product + word-serial Montgomery reduction (variants 3 and 4).
+// A 32x32->64 multiply costs two to three times an add on the integer pipes
+// of sm_103a, so trading products for additions pays: one Karatsuba level
+// turns the 64 products of an 8x8-limb schoolbook into 48, two levels into 36.
+// Carries are tracked in 64-bit C arithmetic (the compiler picks the wide
+// multiply-add forms); the same code runs on the host for testing.
+// ---------------------------------------------------------------------------
+// r[0..2n) = a[0..n) * b[0..n), schoolbook
+template <int NL>
+PP_HD void mul_school(uint32_t *r, const uint32_t *a, const uint32_t *b) {
+#pragma unroll
+  for (int k = 0; k < 2 * NL; ++k) r[k] = 0;
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    uint64_t c = 0;
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+      const uint64_t s = (uint64_t)a[i] * b[j] + r[i + j] + c;
+      r[i + j] = (uint32_t)s;
+      c = s >> 32;
+    }
+    r[i + NL] = (uint32_t)c;
+  }
+}
+
+// r[0..2n) = a * b via one Karatsuba level on top of MUL (n = 2h)
+template <int NL, bool DEEP>
+PP_HD void mul_kara(uint32_t *r, const uint32_t *a, const uint32_t *b) {
+  constexpr int H = NL / 2;
+  uint32_t sa[H], sb[H];
+  uint64_t c = 0;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    c += (uint64_t)a[i] + a[i + H];
+    sa[i] = (uint32_t)c;
+    c >>= 32;
+  }
+  const uint32_t ca = (uint32_t)c;
+  c = 0;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    c += (uint64_t)b[i] + b[i + H];
+    sb[i] = (uint32_t)c;
+    c >>= 32;
+  }
+  const uint32_t cb = (uint32_t)c;
+  uint32_t z0[NL], z2[NL], z1[NL];
+  if constexpr (DEEP && (H % 2 == 0)) {
+    mul_kara<H, false>(z0, a, b);
+    mul_kara<H, false>(z2, a + H, b + H);
+    mul_kara<H, false>(z1, sa, sb);
+  } else {
+    mul_school<H>(z0, a, b);
+    mul_school<H>(z2, a + H, b + H);
+    mul_school<H>(z1, sa, sb);
+  }
+  // z1 (NL+1 limbs) += ca*sb<<H*32 + cb*sa<<H*32 + ca*cb<<NL*32
+  const uint32_t ma = 0u - ca, mb = 0u - cb;
+  uint32_t z1top = ca & cb;
+  c = 0;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    c += (uint64_t)z1[i + H] + (sb[i] & ma) + (sa[i] & mb);
+    z1[i + H] = (uint32_t)c;
+    c >>= 32;
+  }
+  z1top += (uint32_t)c;
+  // z1 -= z0 + z2 (the middle term is non-negative)
+  int64_t br = 0;
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    const int64_t d = (int64_t)z1[i] - z0[i] - z2[i] + br;
+    z1[i] = (uint32_t)d;
+    br = d >> 32;  // arithmetic: -2, -1 or 0
+  }
+  z1top = (uint32_t)((int64_t)z1top + br);
+  // r = z0 + z1 << (H*32) + z2 << (NL*32)
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    r[i] = z0[i];
+    r[i + NL] = z2[i];
+  }
+  c = 0;
+#pragma unroll
+  for (int i = 0; i < NL; ++i) {
+    c += (uint64_t)r[i + H] + z1[i];
+    r[i + H] = (uint32_t)c;
+    c >>= 32;
+  }
+  c += (uint64_t)r[NL + H] + z1top;
+  r[NL + H] = (uint32_t)c;
+  c >>= 32;
+#pragma unroll
+  for (int i = NL + H + 1; i < 2 * NL; ++i) {
+    c += r[i];
+    r[i] = (uint32_t)c;
+    c >>= 32;
+  }
+}
+
+// Word-serial Montgomery reduction of t[0..16) (t < r * 2^256):
+// t * 2^-256 mod r.  Round i adds m * r * 2^(32 i) with m = -t[i]; r[0] = 1
+// and r[1] = 2^32 - 1 make the first two word products shifts and adds
+// (m * (2^32 - 1) = (m << 32) - m), so a round costs 6 wide products.  The
+// carry out of round i's top word (i + 8) is kept as one bit and added with
+// round i+1's carry into word i + 9, so no carry ripples to the top.
+PP_HD fr mont_redc16(uint32_t t[16]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  uint32_t hc = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t m = 0u - t[i];
+    uint64_t c = ((uint64_t)m + t[i]) >> 32;  // word i becomes 0
+    uint64_t s = ((uint64_t)m << 32) - m + t[i + 1] + c;
+    t[i + 1] = (uint32_t)s;
+    c = s >> 32;
+#pragma unroll
+    for (int j = 2; j < 8; ++j) {
+      s = (uint64_t)m * r[j] + t[i + j] + c;
+      t[i + j] = (uint32_t)s;
+      c = s >> 32;
+    }
+    s = (uint64_t)t[i + 8] + c + hc;
+    t[i + 8] = (uint32_t)s;
+    hc = (uint32_t)(s >> 32);
+  }
+  // result t[8..16) < 2r < 2^256 (hc == 0)
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[8 + i];
+  fr_reduce_once(out.v);
+  return out;
+}
+
+// variant 3: one Karatsuba level; variant 4: two levels
+template <bool DEEP>
+PP_HD fr fr_mul_kara(const fr &a, const fr &b) {
+  uint32_t t[16];
+  mul_kara<8, DEEP>(t, a.v, b.v);
+  return mont_redc16(t);
+}
+
 #ifndef PP_MUL_VARIANT
 #define PP_MUL_VARIANT 0
 #endif
 
+// variant 5: schoolbook product + the same reduction (separated operand scanning)
+PP_HD fr fr_mul_sos(const fr &a, const fr &b) {
+  uint32_t t[16];
+  mul_school<8>(t, a.v, b.v);
+  return mont_redc16(t);
+}
+
 PP_HD fr fr_mul(const fr &a, const fr &b) {
 #if PP_MUL_VARIANT == 2
   return fr_mul_w(a, b);
+#elif PP_MUL_VARIANT == 3
+  return fr_mul_kara<false>(a, b);
+#elif PP_MUL_VARIANT == 4
+  return fr_mul_kara<true>(a, b);
+#elif PP_MUL_VARIANT == 5
+  return fr_mul_sos(a, b);
 #else
   return fr_mul_v<PP_MUL_VARIANT>(a, b);
 #endif

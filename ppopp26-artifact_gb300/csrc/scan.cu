@@ -97,7 +97,10 @@ __global__ void __launch_bounds__(kScanThreads) k_gp_local(const fr *__restrict_
   if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blockIdx.x, incl);
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_gp_apply(fr *inout, ScanGeom g,
+// out_excl[i] = prod_{j<i} in[j] and/or out_incl[i] = prod_{j<=i} in[j]; either
+// output may be null or alias `in` (each element is read before it is written)
+__global__ void __launch_bounds__(kScanThreads) k_gp_apply(const fr *in, fr *out_excl, fr *out_incl,
+                                                            ScanGeom g,
                                                             const fr *__restrict__ thread_excl,
                                                             const fr *__restrict__ block_total) {
   __shared__ fr s[kScanThreads];
@@ -116,9 +119,10 @@ __global__ void __launch_bounds__(kScanThreads) k_gp_apply(fr *inout, ScanGeom g
   fr run = fr_mul(block_prefix, ld_fr(thread_excl + gt));
   const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
   for (uint64_t i = lo; i < hi; ++i) {
-    const fr v = ld_fr(inout + i);
-    st_fr(inout + i, run);
+    const fr v = ld_fr(in + i);
+    if (out_excl) st_fr(out_excl + i, run);
     run = fr_mul(run, v);
+    if (out_incl) st_fr(out_incl + i, run);
   }
 }
 
@@ -304,10 +308,11 @@ static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 
 
 using pp::fr;
 
-extern "C" int pp_gp_prefix(void *d_inout, uint64_t n, void *stream) {
+extern "C" int pp_gp_scan(const void *d_in, void *d_excl, void *d_incl, uint64_t n, void *stream) {
   if (n == 0) return PP_OK;
-  if (!d_inout || !pp::aligned16(d_inout)) {
-    pp::set_error("pp_gp_prefix: buffer must be a 16-byte aligned device pointer");
+  if (!d_in || !pp::aligned16(d_in) || (d_excl && !pp::aligned16(d_excl)) ||
+      (d_incl && !pp::aligned16(d_incl)) || (!d_excl && !d_incl)) {
+    pp::set_error("pp_gp_scan: need a 16-byte aligned input and at least one aligned output");
     return PP_E_INVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
@@ -317,15 +322,24 @@ extern "C" int pp_gp_prefix(void *d_inout, uint64_t n, void *stream) {
       pp::workspace_get((g.threads + g.blocks) * sizeof(fr), s, 1, &st));
   if (st) return st;
   fr *thread_excl = ws, *block_total = ws + g.threads;
-  pp::k_gp_local<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<fr *>(d_inout), g, thread_excl,
+  pp::k_gp_local<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<const fr *>(d_in), g, thread_excl,
                                                        block_total);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<fr *>(d_inout), g, thread_excl,
-                                                       block_total);
+  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(
+      static_cast<const fr *>(d_in), static_cast<fr *>(d_excl), static_cast<fr *>(d_incl), g,
+      thread_excl, block_total);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
+}
+
+extern "C" int pp_gp_prefix(void *d_inout, uint64_t n, void *stream) {
+  if (n && (!d_inout || !pp::aligned16(d_inout))) {
+    pp::set_error("pp_gp_prefix: buffer must be a 16-byte aligned device pointer");
+    return PP_E_INVAL;
+  }
+  return pp_gp_scan(d_inout, d_inout, nullptr, n, stream);
 }
 
 extern "C" int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *stream) {
@@ -420,7 +434,8 @@ extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, co
   pp::k_perm_local<<<g.blocks, pp::kScanThreads, 0, s>>>(a, g, thread_excl, block_total);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a.z, g, thread_excl, block_total);
+  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a.z, a.z, nullptr, g, thread_excl,
+                                                       block_total);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;

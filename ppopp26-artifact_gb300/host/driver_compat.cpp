@@ -1,0 +1,126 @@
+// driver_compat.cpp -- command-line driver over the reference-compatible host
+// layer, in the shape of the reference's drivers (miss_ops.cu, ntt.cu
+// --check-*, lde.cu --bench).  Inputs and outputs are raw files of 32-byte
+// Montgomery elements, the format of the reference's input.bin.
+//
+//   pp_compat_driver miss_ops <lg_N> <in.bin> <outdir>
+//       accumulate_mul_poly, accumulate_mul_poly_, evaluate, poly_div_poly on
+//       the input (point and divisor constants of miss_ops.cu:133-135,
+//       :180-183) -> <outdir>/{gp,gp_incl,eval,div}.bin
+//   pp_compat_driver ntt <lg_N> <in.bin> <out.bin>
+//       Ntt::forward -> out.bin; checks our_ntt and standard4_ntt against it
+//       byte for byte and Intt::forward against the input (ntt.cu:1276-1351)
+//   pp_compat_driver lde <lg_N> <lambda> <in.bin> <out.bin> [naive]
+//       our_lde (or naive_lde) -> out.bin
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "function.h"
+
+static std::vector<unsigned char> read_file(const std::string &path, size_t bytes) {
+  std::vector<unsigned char> v(bytes);
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) throw pp::Error(1, "cannot open " + path);
+  const size_t got = std::fread(v.data(), 1, bytes, f);
+  std::fclose(f);
+  if (got != bytes) throw pp::Error(1, "short read from " + path);
+  return v;
+}
+
+static void write_file(const std::string &path, const void *p, size_t bytes) {
+  FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) throw pp::Error(1, "cannot create " + path);
+  std::fwrite(p, 1, bytes, f);
+  std::fclose(f);
+}
+
+static SyncedMemory load(const std::string &path, size_t n) {
+  SyncedMemory m(n * 32);
+  auto v = read_file(path, n * 32);
+  std::memcpy(m.mutable_cpu_data(), v.data(), n * 32);
+  return m;
+}
+
+static int miss_ops(int lg, const std::string &in, const std::string &outdir) {
+  const size_t n = size_t{1} << lg;
+  SyncedMemory gp = load(in, n);
+  SyncedMemory incl(n * 32);
+  SyncedMemory gp2 = load(in, n);
+  accumulate_mul_poly(gp);
+  accumulate_mul_poly_(gp2, incl);
+  cudaDeviceSynchronize();
+  if (std::memcmp(gp.mutable_cpu_data(), gp2.mutable_cpu_data(), n * 32) != 0) {
+    std::printf("accumulate_mul_poly and accumulate_mul_poly_ disagree\n");
+    return 2;
+  }
+  write_file(outdir + "/gp.bin", gp.mutable_cpu_data(), n * 32);
+  write_file(outdir + "/gp_incl.bin", incl.mutable_cpu_data(), n * 32);
+
+  SyncedMemory point(32);
+  const uint64_t pt[4] = {123456789UL, 987654321UL, 1122334455UL, 6677889900UL};
+  std::memcpy(point.mutable_cpu_data(), pt, 32);
+  SyncedMemory poly = load(in, n);
+  SyncedMemory y = evaluate(poly, point);
+  write_file(outdir + "/eval.bin", y.mutable_cpu_data(), 32);
+
+  SyncedMemory c(32);
+  const uint64_t cv[4] = {123456789123456789UL, 987654321987654321UL, 1122334455667788UL,
+                          1122334455667788UL};
+  std::memcpy(c.mutable_cpu_data(), cv, 32);
+  SyncedMemory div = load(in, n);
+  poly_div_poly(div, c);
+  write_file(outdir + "/div.bin", div.mutable_cpu_data(), n * 32);
+  std::printf("miss_ops ok\n");
+  return 0;
+}
+
+static int ntt_check(int lg, const std::string &in, const std::string &out) {
+  const size_t n = size_t{1} << lg;
+  Ntt ntt(32);
+  Intt intt(32);
+  SyncedMemory x = load(in, n);
+  SyncedMemory expected = ntt.forward(x);
+  cudaDeviceSynchronize();
+  write_file(out, expected.mutable_cpu_data(), n * 32);
+  SyncedMemory a = load(in, n), b = load(in, n);
+  our_ntt(a, lg, lg / 2, lg - lg / 2, 2, 16, 16, ntt);
+  standard4_ntt(b, lg, lg / 2, lg - lg / 2, 2, 16, ntt);
+  const bool ok1 = std::memcmp(a.mutable_cpu_data(), expected.mutable_cpu_data(), n * 32) == 0;
+  const bool ok2 = std::memcmp(b.mutable_cpu_data(), expected.mutable_cpu_data(), n * 32) == 0;
+  SyncedMemory back = intt.forward(expected);
+  cudaDeviceSynchronize();
+  const bool ok3 = std::memcmp(back.mutable_cpu_data(), x.mutable_cpu_data(), n * 32) == 0;
+  std::printf("check our_ntt: %s, standard4_ntt: %s, intt round trip: %s\n", ok1 ? "ok" : "MISMATCH",
+              ok2 ? "ok" : "MISMATCH", ok3 ? "ok" : "MISMATCH");
+  return ok1 && ok2 && ok3 ? 0 : 2;
+}
+
+static int lde(int lg, int lambda, const std::string &in, const std::string &out, bool naive) {
+  const size_t n = size_t{1} << lg;
+  auto v = read_file(in, n * 32);
+  Ntt ntt(32);
+  auto *p = reinterpret_cast<cpu::BLS12_381_Fr_G1 *>(v.data());
+  const float ms = naive ? naive_lde(p, lg, lambda, 1, 16, 16, ntt) : our_lde(p, lg, lambda, 1, 16, 16, ntt);
+  SyncedMemory o = last_lde_output();
+  write_file(out, o.mutable_cpu_data(), o.size());
+  std::printf("lde ok %.3f ms\n", ms);
+  return 0;
+}
+
+int main(int argc, char **argv) {
+  try {
+    if (argc >= 5 && std::string(argv[1]) == "miss_ops") return miss_ops(std::atoi(argv[2]), argv[3], argv[4]);
+    if (argc >= 5 && std::string(argv[1]) == "ntt") return ntt_check(std::atoi(argv[2]), argv[3], argv[4]);
+    if (argc >= 6 && std::string(argv[1]) == "lde")
+      return lde(std::atoi(argv[2]), std::atoi(argv[3]), argv[4], argv[5],
+                 argc >= 7 && std::string(argv[6]) == "naive");
+  } catch (const pp::Error &e) {
+    std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
+    return 3;
+  }
+  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde ...\n", argv[0]);
+  return 1;
+}

@@ -1,0 +1,65 @@
+"""The reference-compatible C++ host layer (SyncedMemory, Ntt/Intt,
+accumulate_mul_poly, evaluate, poly_div_poly, our_ntt, standard4_ntt,
+our_lde, naive_lde) driven like the reference's own drivers, on raw files of
+Montgomery elements, checked against the oracle."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+DRIVER = os.path.join(ROOT, "ppopp26-artifact_gb300", "pp_compat_driver")
+
+
+def run(*args):
+    r = subprocess.run([DRIVER, *map(str, args)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+def load(path, n):
+    return np.fromfile(path, dtype=np.uint64).reshape(n, 4)
+
+
+@pytest.mark.parametrize("lg", [1, 10, 16])
+def test_miss_ops_driver(pp, O, cuda, tmp_path, lg):
+    n = 1 << lg
+    x = O.random_fr(n, 4000 + lg)
+    x.tofile(tmp_path / "in.bin")
+    run("miss_ops", lg, tmp_path / "in.bin", tmp_path)
+    assert O.first_diff(load(tmp_path / "gp.bin", n), O.gp_prefix(x)) == -1
+    incl = O.gp_prefix(x)
+    incl = np.array([O.fr_mul(incl[i], x[i]) for i in range(n)]) if n <= 1024 else None
+    if incl is not None:
+        assert O.first_diff(load(tmp_path / "gp_incl.bin", n), incl) == -1
+    pt = np.array([123456789, 987654321, 1122334455, 6677889900], np.uint64)
+    assert (load(tmp_path / "eval.bin", 1)[0] == O.evaluate(x, pt)).all()
+    c = np.array([123456789123456789, 987654321987654321, 1122334455667788, 1122334455667788], np.uint64)
+    assert O.first_diff(load(tmp_path / "div.bin", n), O.div_xplusc(x, c)) == -1
+
+
+@pytest.mark.parametrize("lg", [3, 12, 20])
+def test_ntt_driver_checks(pp, O, cuda, tmp_path, lg):
+    n = 1 << lg
+    x = O.random_fr(n, 5000 + lg)
+    x.tofile(tmp_path / "in.bin")
+    out = run("ntt", lg, tmp_path / "in.bin", tmp_path / "out.bin")
+    assert "our_ntt: ok, standard4_ntt: ok, intt round trip: ok" in out
+    assert O.first_diff(load(tmp_path / "out.bin", n), O.ntt(x)) == -1
+
+
+@pytest.mark.parametrize("lg,lam", [(8, 2), (16, 3)])
+def test_lde_driver(pp, O, cuda, tmp_path, lg, lam):
+    n = 1 << lg
+    x = O.random_fr(n, 6000 + lg)
+    x.tofile(tmp_path / "in.bin")
+    run("lde", lg, lam, tmp_path / "in.bin", tmp_path / "out.bin")
+    assert O.first_diff(load(tmp_path / "out.bin", n << lam), O.lde_coeffs(x, lam)) == -1
+    run("lde", lg, lam, tmp_path / "in.bin", tmp_path / "out2.bin", "naive")
+    assert O.first_diff(load(tmp_path / "out2.bin", n << lam), O.lde_spread(x, lam)) == -1
