@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-ops", action="store_true", help="skip the secondary operator timings")
+    ap.add_argument("--lean", action="store_true",
+                    help="device timing only (no e2e, CPU baseline, ops): the profiling case")
+    ap.add_argument("--lg", type=int, default=LG_N, help="transform size (profiling of smaller cases)")
     return ap.parse_args()
 
 
@@ -202,17 +205,19 @@ def run_ours(args, rank, world, local):
             dist.barrier()
 
     # ---- device-resident headline
-    x = pp.random_fr(N, 0x5EED0018 + rank)
-    out = ppfr.empty(N)
-    ppfr.prepare(LG_N, False)
+    n = 1 << args.lg
+    x = pp.random_fr(n, 0x5EED0018 + rank)
+    out = ppfr.empty(n)
+    ppfr.prepare(args.lg, False)
     fn = lambda: pp.ntt(x, out=out)  # noqa: E731
     for _ in range(args.warmup):
         fn()
     torch.cuda.synchronize()
     barrier()
     clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
+    if not args.lean:
+        clocks.start()
+        time.sleep(0.3)
     launches0 = pp.launch_count()
     torch.cuda.synchronize()
     barrier()
@@ -220,6 +225,16 @@ def run_ours(args, rank, world, local):
     launches = pp.launch_count() - launches0
     torch.cuda.synchronize()
     barrier()
+    if args.lean or args.lg != LG_N:
+        # profiling case: device time only
+        if rank == 0:
+            print(json.dumps({"metric": "fr_ntt_2^%d_throughput" % args.lg, "lean": True,
+                              "value": round(n * args.steps / (ms / 1e3) / 1e6, 3), "unit": "Melem/s",
+                              "ms_per_step": round(ms / args.steps, 4), "gpu_launches": int(launches)}),
+                  flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
     # ---- end to end through the C ABI with host buffers
     hin = torch.empty((N, 4), dtype=torch.int64, pin_memory=True)
     hin.copy_(x.cpu())

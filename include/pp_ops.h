@@ -48,6 +48,12 @@ const char *pp_version(void);
  * (ntt.cu:1039-1138) reproduce bit for bit.  0 <= lg_n <= PP_MAX_LG_N. */
 int pp_ntt(const void *d_in, void *d_out, uint32_t lg_n, int inverse, void *stream);
 
+/* Builds (synchronously) the cached twiddle tables of a transform size so
+ * that later pp_ntt calls of that size only launch the pass kernels (e.g.
+ * before CUDA-graph capture).  The reference builds its table blob in the
+ * Ntt constructor (function.cu:278 -> zksnark_ntt.cu:17-39). */
+int pp_ntt_prepare(uint32_t lg_n, int inverse);
+
 /* ---------------------------------------------------------------- LDE ---
  * Low-degree extension onto 2^(lg_n+lambda) points, natural order out.
  *  mode 0 (PP_LDE_COEFFS): d_in holds 2^lg_n coefficients a_i; output is
