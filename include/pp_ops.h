@@ -100,6 +100,21 @@ int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, const void *d
  * mont_arithmetic.cu:104-163, :507-529). */
 int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_y, void *stream);
 
+/* pp_eval for callers that must not allocate device memory during the call:
+ * processes whose device memory is all reserved by their own pool, and
+ * latency-critical loops that cannot absorb the device-wide synchronisation
+ * cudaMalloc/cudaFree may cause.  No reference counterpart: the reference's
+ * evaluate allocates a power table and partial sums on every call.
+ * Its scratch is a static 64 KiB device array (present on every device that
+ * loads the library, until exit), so n <= PP_EVAL_NOALLOC_MAX_N (2^22);
+ * larger n returns PP_E_UNSUPPORTED.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress, no allocation); make that first
+ * call before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (e.g. on two streams) race and must be ordered by the
+ * caller.  Same result as pp_eval, bit for bit. */
+#define PP_EVAL_NOALLOC_MAX_N (1ull << 22)
+int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, void *d_y, void *stream);
+
 /* ----------------------------------------------------------- division ---
  * In place: the buffer p (n coefficients) becomes q with q_i = S_{i+1},
  * S_i = sum_{j>=i} p_j (-c)^(j-i), q_{n-1} = 0 -- the quotient of p by (X + c)

@@ -18,6 +18,8 @@
 #include "common.cuh"
 #include "ntt.cuh"
 
+#include <mutex>
+
 namespace pp {
 
 constexpr int kScanThreads = 256;
@@ -436,6 +438,99 @@ extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, co
   PP_LAUNCH_CHECK();
   pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a.z, a.z, nullptr, g, thread_excl,
                                                        block_total);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation that allocates nothing.
+//
+// pp_eval takes its block summaries from a per-stream workspace that is
+// created with cudaMalloc on first use.  Some callers cannot allow that: a
+// serving process that has handed all free device memory to its own pool
+// (a fresh cudaMalloc would fail or fragment it), or a latency-critical loop
+// where cudaMalloc / cudaFree may synchronise the whole device and stall the
+// work of other streams.  For them pp_eval_noalloc keeps its scratch in a
+// file-scope device array that exists, for every device that loads this
+// library, from module load until process exit:
+//   2 * 1024 block summaries of 32 bytes = 64 KiB per device.
+// With 16 elements per thread and 256 threads per block that bounds the
+// polynomial at 1024 * 256 * 16 = 2^22 coefficients; longer ones are refused
+// with PP_E_UNSUPPORTED before any device work.
+// ---------------------------------------------------------------------------
+namespace pp {
+
+constexpr uint32_t kEvalNoAllocMaxBlocks = 1024;
+constexpr uint64_t kEvalNoAllocChunk = 16;
+static_assert((uint64_t)kEvalNoAllocMaxBlocks * kScanThreads * kEvalNoAllocChunk == PP_EVAL_NOALLOC_MAX_N,
+              "header limit and scratch geometry disagree");
+
+// [0, 1024): affine-map offsets a_b of the blocks, [1024, 2048): factors b_b
+static __device__ __align__(256) fr g_eval_noalloc_scratch[2 * kEvalNoAllocMaxBlocks];
+
+// device address of g_eval_noalloc_scratch, looked up once per device
+static std::mutex g_eval_noalloc_mu;
+static fr *g_eval_noalloc_addr[64] = {nullptr};
+
+}  // namespace pp
+
+extern "C" int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, void *d_y,
+                               void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!d_y || !pp::aligned16(d_y) || (n && (!d_poly || !d_x || !pp::aligned16(d_poly) ||
+                                            !pp::aligned16(d_x)))) {
+    pp::set_error("pp_eval_noalloc: buffers must be 16-byte aligned device pointers");
+    return PP_E_INVAL;
+  }
+  if (n > PP_EVAL_NOALLOC_MAX_N) {
+    pp::set_error("pp_eval_noalloc: %llu coefficients exceed the 2^22 its static scratch covers; "
+                  "use pp_eval",
+                  (unsigned long long)n);
+    return PP_E_UNSUPPORTED;
+  }
+  if (n == 0) {
+    pp::k_zero1<<<1, 1, 0, s>>>(static_cast<fr *>(d_y));
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    return PP_OK;
+  }
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    pp::set_error("pp_eval_noalloc: device index %d out of range", dev);
+    return PP_E_INVAL;
+  }
+  fr *scratch = nullptr;
+  {
+    // set-up on the first call on this device (that device is current): the
+    // host-side name of the array is not a device address; ask the runtime
+    std::lock_guard<std::mutex> lk(pp::g_eval_noalloc_mu);
+    if (!pp::g_eval_noalloc_addr[dev]) {
+      void *p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, pp::g_eval_noalloc_scratch);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        pp::set_error("pp_eval_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        return PP_E_CUDA;
+      }
+      pp::g_eval_noalloc_addr[dev] = static_cast<fr *>(p);
+    }
+    scratch = pp::g_eval_noalloc_addr[dev];
+  }
+  pp::ScanGeom g;
+  g.n = n;
+  g.k = pp::kEvalNoAllocChunk;
+  g.threads = (n + g.k - 1) / g.k;
+  g.blocks = (uint32_t)((g.threads + pp::kScanThreads - 1) / pp::kScanThreads);
+  // every block summary read by k_eval_final is written by k_affine_local in
+  // the same call, so nothing in the array has to be cleared first
+  fr *ba = scratch, *bb = scratch + pp::kEvalNoAllocMaxBlocks;
+  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(
+      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), 0, nullptr, nullptr, ba, bb);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_eval_final<<<1, pp::kScanThreads, 0, s>>>(ba, bb, g.blocks, static_cast<fr *>(d_y));
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
