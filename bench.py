@@ -42,7 +42,7 @@ IMAD_PER_CLK_PER_SM = 64               # 32-bit multiply-add lanes per SM per cl
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-ops", action="store_true", help="skip the secondary operator timings")
@@ -75,7 +75,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
@@ -247,15 +247,51 @@ def run_ours(args, rank, world, local):
         hout.copy_(dbuf, non_blocking=True)
 
     e2e_steps = max(3, args.steps // 2)
-    e2e_ms = time_device(e2e_step, e2e_steps, 1, torch)
+    e2e_serial_ms = time_device(e2e_step, e2e_steps, 1, torch)
+    # streaming form: step i's H2D, transform and D2H on three streams with two
+    # device buffers, so copies of neighbouring steps overlap the transform
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    s_cmp = torch.cuda.current_stream()
+    dbufs = [dbuf, ppfr.empty(n)]
+    houts = [hout, torch.empty_like(hin, pin_memory=True)]
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_cmp = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+
+    def e2e_stream(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s_in)
+        for i in range(steps):
+            b = i % 2
+            if i >= 2:
+                s_in.wait_event(ev_out[b])
+            with torch.cuda.stream(s_in):
+                dbufs[b].copy_(hin, non_blocking=True)
+            ev_in[b].record(s_in)
+            s_cmp.wait_event(ev_in[b])
+            pp.ntt(dbufs[b], out=dbufs[b], stream=s_cmp)
+            ev_cmp[b].record(s_cmp)
+            s_out.wait_event(ev_cmp[b])
+            with torch.cuda.stream(s_out):
+                houts[b].copy_(dbufs[b], non_blocking=True)
+            ev_out[b].record(s_out)
+        e1.record(s_out)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    e2e_stream(2)
+    e2e_ms = e2e_stream(e2e_steps)
     clk = clocks.stop()
     # max over ranks
-    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps], dtype=torch.float64, device="cuda")
+    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps, e2e_serial_ms / e2e_steps * args.steps],
+                     dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms_norm = float(t[0]), float(t[1])
+    ms, e2e_ms_norm, e2e_serial_norm = float(t[0]), float(t[1]), float(t[2])
     value = N * args.steps * world / (ms / 1e3) / 1e6
     e2e_value = N * args.steps * world / (e2e_ms_norm / 1e3) / 1e6
+    e2e_serial_value = N * args.steps * world / (e2e_serial_norm / 1e3) / 1e6
 
     ops = {}
     if not args.no_ops and rank == 0:
@@ -273,7 +309,7 @@ def run_ours(args, rank, world, local):
     achieved_int = MM_PER_NTT * INSTR_PER_MM / sec_per_ntt / 1e12
     achieved_hbm = BYTES_PER_NTT / sec_per_ntt / 1e9
     # one NTT is len(split) kernel launches; per-launch figures are the same ratio
-    traffic = profile_traffic("ntt_pass_2p24_traffic.txt")
+    traffic = profile_traffic("ntt_pass_2p24_launches.md")
     cpu_rate, cpu_dt = cpu_ntt_rate(LG_N, 2, os.cpu_count() or 1)
     line = {
         "metric": "fr_ntt_2^24_throughput", "value": round(value, 3), "unit": "Melem/s",
@@ -283,7 +319,9 @@ def run_ours(args, rank, world, local):
         "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N,
                    "l2_flush": "not needed: 512 MiB input > 129 MB L2", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Melem/s", "h2d_bytes_per_step": 32 * N,
-                "d2h_bytes_per_step": 32 * N},
+                "d2h_bytes_per_step": 32 * N, "steps": e2e_steps,
+                "form": "streamed: H2D / NTT / D2H of neighbouring steps overlap on 3 streams",
+                "serial_value": round(e2e_serial_value, 3)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "k_ntt_pass", "achieved": round(achieved_int, 3),
                      "peak": round(int_peak, 3), "unit": "Tinstr/s", "frac": round(achieved_int / int_peak, 4),
@@ -341,7 +379,127 @@ def secondary_ops(pp, torch):
     params = pp.random_fr(5, 30)
     zz = ppfr.empty(n)
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
+    del w, s, p
+    res["batched"] = batched_bench(pp, torch)
+    res["serving"] = serving_bench(pp, torch)
     return res
+
+
+def batched_bench(pp, torch):
+    """96 polynomials, sizes log-uniform in 2^12..2^22 (seeded): 64 NTT/INTT,
+    24 lambda=2 LDEs, 8 grand products.  Loop of single calls vs one batch
+    plan (a few persistent launches) vs its CUDA-graph replay."""
+    import numpy as np
+
+    P = pp.ppfr
+    rng = np.random.default_rng(0xBA7C4)
+    lgs = [int(v) for v in np.floor(rng.uniform(12, 23, 96))]
+    kinds = [P.JOB_NTT] * 32 + [P.JOB_INTT] * 32 + [P.JOB_LDE_COEFFS] * 24 + [P.JOB_GP] * 8
+    rng.shuffle(kinds)
+    jobs, loop = [], []
+    for i, (k, lg) in enumerate(zip(kinds, lgs)):
+        lam = 2 if k == P.JOB_LDE_COEFFS else 0
+        x = P.random_fr(1 << lg, 0xB000 + i)
+        out = P.empty(1 << (lg + lam))
+        jobs.append((k, x, out, lam))
+        if k == P.JOB_NTT:
+            loop.append(lambda x=x, out=out: P.ntt(x, out=out))
+        elif k == P.JOB_INTT:
+            loop.append(lambda x=x, out=out: P.ntt(x, True, out=out))
+        elif k == P.JOB_LDE_COEFFS:
+            loop.append(lambda x=x, out=out: P.lde(x, 2, P.LDE_COEFFS, out=out))
+        else:
+            loop.append(lambda x=x, out=out: (out.copy_(x), P.gp_prefix_(out)))
+    elems = sum(1 << lg for lg in lgs)
+    l0 = P.launch_count()
+    ms_loop = time_device(lambda: [f() for f in loop], 3, 1, torch) / 3
+    loop_launches = (P.launch_count() - l0) // 4
+    b = P.Batch(jobs)
+    info = b.info()
+    ms_batch = time_device(b.run, 5, 2, torch) / 5
+    b.capture()
+    ms_graph = time_device(b.run, 10, 2, torch) / 10
+    b.close()
+    return {"polys": 96, "input_elems": elems, "loop_ms": round(ms_loop, 3), "batch_ms": round(ms_batch, 3),
+            "graph_ms": round(ms_graph, 3), "loop_launches": int(loop_launches),
+            "batch_launches": info["launches"], "speedup_batch": round(ms_loop / ms_batch, 3),
+            "speedup_graph": round(ms_loop / ms_graph, 3),
+            "Melem_per_s_graph": round(elems / (ms_graph / 1e3) / 1e6, 1)}
+
+
+def serving_bench(pp, torch):
+    """Poisson-arriving prover-round bundles (3 lambda=2 LDEs, 1 grand product,
+    1 division, 6 evaluations), sizes log-uniform in 2^16..2^24, through the
+    continuous-batching server (150 GB budget, 8 slots) vs the same bundles
+    processed one at a time with the plain operators under the same arrivals."""
+    import numpy as np
+
+    P = pp.ppfr
+    rng = np.random.default_rng(0x5E7E)
+    M = 24
+    lgs = [int(v) for v in np.floor(rng.uniform(16, 25, M))]
+    srv = P.Server(budget_bytes=150 * 10**9, slots=8, min_lg=16, max_lg=24, lam=2)
+
+    def serial_one(lg, seed):
+        n = 1 << lg
+        buf = P.empty(7 * n)
+        P.check(P.lib().pp_random_fr(P._ptr(buf), 7 * n, seed, 0, P._stream()))
+        prm = P.empty(12)
+        P.check(P.lib().pp_random_fr(P._ptr(prm), 12, seed ^ 0x9A7A9A7A, 0, P._stream()))
+        w = [buf[j * n:(j + 1) * n] for j in range(3)]
+        s = [buf[(3 + j) * n:(4 + j) * n] for j in range(3)]
+        for j in range(3):
+            P.lde(w[j], 2, P.LDE_COEFFS)
+        P.gp_perm(w, s, prm[:5].contiguous())
+        P.div_xplusc_(buf[6 * n:7 * n], prm[5:6].contiguous())
+        y = P.empty(6)
+        for k in range(6):
+            P.evaluate((w + s)[k], prm[6 + k:7 + k].contiguous(), out=y[k:k + 1])
+        torch.cuda.synchronize()
+
+    # service times of the serial form set the arrival rate (~1.5x its capacity)
+    for lg in sorted(set(lgs)):
+        serial_one(lg, 1)
+    t0 = time.perf_counter()
+    for i, lg in enumerate(lgs):
+        serial_one(lg, 100 + i)
+    serial_total = time.perf_counter() - t0
+    gaps = rng.exponential(serial_total / M / 1.5, M)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    # serial under the arrival process
+    lat = []
+    start = time.perf_counter()
+    for i, lg in enumerate(lgs):
+        now = time.perf_counter() - start
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        serial_one(lg, 100 + i)
+        lat.append((time.perf_counter() - start - arrivals[i]) * 1e3)
+    serial_span = time.perf_counter() - start
+    # the server under the same arrival process
+    for lg in sorted(set(lgs)):  # warm the slot streams
+        srv.release(srv.wait(srv.submit(lg, 1)).ticket)
+    srv.reset_stats()
+    tickets = []
+    start = time.perf_counter()
+    for i, lg in enumerate(lgs):
+        now = time.perf_counter() - start
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        tickets.append(srv.submit(lg, 100 + i))
+    for t in tickets:
+        srv.wait(t, 120000)
+        srv.release(t)
+    st = srv.stats()
+    srv.close()
+    lat.sort()
+    return {"bundles": M, "lg_range": [16, 24],
+            "server": {"bundles_per_s": round(st["bundles_per_s"], 2), "p50_ms": round(st["p50_ms"], 2),
+                       "p99_ms": round(st["p99_ms"], 2), "max_concurrent": int(st["max_concurrent"]),
+                       "admitted_while_busy": int(st["admitted_while_busy"]),
+                       "budget_peak_gb": round(st["budget_peak"] / 1e9, 2)},
+            "serial": {"bundles_per_s": round(M / serial_span, 2), "p50_ms": round(lat[(M - 1) // 2], 2),
+                       "p99_ms": round(lat[int((M - 1) * 0.99)], 2)}}
 
 
 def main():

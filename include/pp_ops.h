@@ -54,6 +54,21 @@ int pp_ntt(const void *d_in, void *d_out, uint32_t lg_n, int inverse, void *stre
  * Ntt constructor (function.cu:278 -> zksnark_ntt.cu:17-39). */
 int pp_ntt_prepare(uint32_t lg_n, int inverse);
 
+/* Radix split of a transform size: bits = 0-terminated pass sizes (log2,
+ * each 3..11, at most 4, summing to lg_n); NULL restores the default.  The
+ * reference fixes its split per kernel (ntt.cuh:113-170; the segmented
+ * drivers take lg_i/lg_k arguments, ntt.cu:979); here it is a tunable. */
+int pp_ntt_set_split(uint32_t lg_n, const uint32_t *bits);
+int pp_ntt_get_split(uint32_t lg_n, uint32_t *bits4);
+/* Times every balanced ordered split of 2^lg_n on the current GPU (CUDA
+ * events, reps calls each), keeps the fastest and returns it (and its time).
+ * Allocates and synchronises: a set-up step, not for hot paths. */
+int pp_ntt_autotune(uint32_t lg_n, int reps, uint32_t *best_bits4, float *best_ms);
+/* Persist / restore the chosen splits as JSON keyed by GPU name
+ * ({"gpu": ..., "ntt": {"<lg>": [k1, ...]}}); load ignores another GPU's file. */
+int pp_tune_save(const char *path);
+int pp_tune_load(const char *path);
+
 /* ---------------------------------------------------------------- LDE ---
  * Low-degree extension onto 2^(lg_n+lambda) points, natural order out.
  *  mode 0 (PP_LDE_COEFFS): d_in holds 2^lg_n coefficients a_i; output is
@@ -123,12 +138,97 @@ int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, void *d_y, 
  * mont_arithmetic.cu:305-331, :531-542).  n >= 1. */
 int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *stream);
 
+/* -------------------------------------------------------------- batch ---
+ * Many polynomials of uneven power-of-two sizes in one plan: every transform
+ * job is split into its passes, and each pass level of the whole batch is one
+ * persistent launch over the tiles of all jobs at that level; grand products
+ * run as two launches over all of them.  A plan owns its workspaces and
+ * descriptors (allocated by pp_batch_create), so pp_batch_run allocates
+ * nothing; pp_batch_capture records the run as a CUDA graph that later
+ * pp_batch_run calls replay.  Buffers are fixed at creation.  The reference
+ * has no batched form: each of its operators is one call per polynomial. */
+#define PP_JOB_NTT 0        /* d_out = NTT(d_in), 2^lg_n points */
+#define PP_JOB_INTT 1       /* d_out = INTT(d_in) */
+#define PP_JOB_LDE_COEFFS 2 /* as pp_lde mode 0, 2^(lg_n+lambda) outputs */
+#define PP_JOB_LDE_EVALS 3  /* as pp_lde mode 1 */
+#define PP_JOB_LDE_SPREAD 4 /* as pp_lde mode 2 */
+#define PP_JOB_GP 5         /* d_out = exclusive prefix product of d_in (may alias) */
+typedef struct pp_job {
+  const void *d_in;
+  void *d_out;
+  uint32_t lg_n;
+  uint32_t kind;
+  uint32_t lambda; /* LDE jobs only */
+  uint32_t reserved;
+} pp_job;
+int pp_batch_create(const pp_job *jobs, uint32_t count, void **plan);
+int pp_batch_run(void *plan, void *stream);
+int pp_batch_capture(void *plan);
+/* launches per run, tiles of all transform levels, number of levels */
+int pp_batch_info(void *plan, uint32_t *launches, uint64_t *tiles, uint32_t *levels);
+int pp_batch_destroy(void *plan);
+
+/* ------------------------------------------------------------ serving ---
+ * Continuous-batching request loop for prover-round bundles.  A bundle on
+ * 2^lg_n-coefficient polynomials is: 3 coset LDEs (mode 0) of the wires w_j,
+ * the copy-constraint grand product z of (w, sigma), the quotient of a
+ * polynomial by (X + c), and 6 evaluations (w_1..3, sigma_1..3 at z_1..6).
+ * Inputs are 7 * 2^lg_n elements (w1..3, sigma1..3, the polynomial to divide)
+ * and 12 parameters (beta, gamma, k1..3, c, z1..6), copied from pinned host
+ * memory or generated on the device from `seed` when the pointers are NULL.
+ * A scheduler thread admits queued bundles whenever one of `slots` streams is
+ * free and the bundle's memory fits in `budget_bytes`; admitted bundles run
+ * concurrently.  Tables and workspaces for lg in [min_lg, max_lg] are built
+ * at creation and stay resident; results stay on the device until
+ * pp_server_release.  All waits are bounded.  No reference counterpart: the
+ * reference runs one operator call at a time on the default stream. */
+typedef struct pp_server_config {
+  uint64_t budget_bytes; /* device memory for bundle buffers (admission limit) */
+  uint32_t slots;        /* concurrent bundles (one stream each), 1..64 */
+  uint32_t min_lg, max_lg;
+  uint32_t lambda;       /* LDE blowup of every bundle */
+  uint32_t max_queue;    /* 0 = unbounded; else pp_server_submit returns PP_E_BUSY when full */
+} pp_server_config;
+typedef struct pp_bundle {
+  uint32_t lg_n;
+  uint32_t lambda;
+  uint64_t seed;
+  const void *h_inputs; /* pinned host, 7 * 2^lg_n elements, or NULL */
+  const void *h_params; /* pinned host, 12 elements, or NULL */
+} pp_bundle;
+typedef struct pp_bundle_result {
+  uint64_t ticket;
+  int status;
+  double latency_ms; /* submit -> completion seen by the scheduler */
+  double queue_ms;   /* submit -> admission */
+  void *d_lde[3];    /* 2^(lg_n+lambda) each */
+  void *d_z;         /* 2^lg_n */
+  void *d_quotient;  /* 2^lg_n (top entry 0) */
+  void *d_evals;     /* 6 */
+  void *d_w[3], *d_sigma[3], *d_params;
+} pp_bundle_result;
+typedef struct pp_server_stats {
+  uint64_t completed, queued, budget_used, budget_peak, admitted_while_busy, max_concurrent;
+  double p50_ms, p99_ms, bundles_per_s;
+} pp_server_stats;
+int pp_server_create(const pp_server_config *cfg, void **server);
+int pp_server_submit(void *server, const pp_bundle *bundle, uint64_t *ticket);
+int pp_server_wait(void *server, uint64_t ticket, int timeout_ms, pp_bundle_result *result);
+int pp_server_release(void *server, uint64_t ticket);
+int pp_server_cancel(void *server, uint64_t ticket);
+int pp_server_get_stats(void *server, pp_server_stats *stats);
+int pp_server_reset_stats(void *server);
+int pp_server_destroy(void *server);
+
 /* ----------------------------------------------------------- utilities --- */
 /* n seeded uniformly random canonical elements: element (first_index + i)
  * limb j is the SplitMix64 output at counter ((first_index+i) << 8 | t << 2 | j)
  * of the stream seeded with seed, bit 255 cleared, rejection-sampled < r
  * (attempt t), stored as the Montgomery representation. */
 int pp_random_fr(void *d_out, uint64_t n, uint64_t seed, uint64_t first_index, void *stream);
+
+/* synchronous device -> host copy (for callers without their own CUDA binding) */
+int pp_copy_to_host(void *h_dst, const void *d_src, uint64_t bytes);
 
 /* number of kernel launches this library has issued from the calling process */
 uint64_t pp_launch_count(void);

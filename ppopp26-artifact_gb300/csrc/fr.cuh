@@ -537,6 +537,195 @@ PP_HD fr fr_mul_kara(const fr &a, const fr &b) {
 #define PP_MUL_VARIANT 0
 #endif
 
+// ---------------------------------------------------------------------------
+// Variants 6-8: bare 32x32->64 products (mul.wide, no addend) whose halves
+// are summed by explicit add-with-carry chains.  On sm_103a a wide multiply
+// with a 64-bit addend occupies the integer-multiply pipe ~1.4x longer than a
+// bare one, while carry-chain adds can issue on the ALU pipe; splitting the
+// two moves work off the multiply pipe, which bounds every other variant.
+// ---------------------------------------------------------------------------
+// t[0..9] += ai * b (one CIOS row, product part) with bare wide products
+PP_HD void row_ab_wide(uint32_t t[10], uint32_t ai, const uint32_t b[8]) {
+  uint32_t lo[8], hi[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint64_t p = (uint64_t)ai * b[j];
+    lo[j] = (uint32_t)p;
+    hi[j] = (uint32_t)(p >> 32);
+  }
+  t[0] = add_cc(t[0], lo[0]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j] = addc_cc(t[j], lo[j]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[1] = add_cc(t[1], hi[0]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j + 1] = addc_cc(t[j + 1], hi[j]);
+  t[9] = addc(t[9], 0);
+}
+
+// same product part with lo/hi multiply-add carry chains (as variant 0)
+PP_HD void row_ab_madc(uint32_t t[10], uint32_t ai, const uint32_t b[8]) {
+  t[0] = madlo_cc(ai, b[0], t[0]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j] = madloc_cc(ai, b[j], t[j]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[1] = madhi_cc(ai, b[0], t[1]);
+#pragma unroll
+  for (int j = 1; j < 8; ++j) t[j + 1] = madhic_cc(ai, b[j], t[j + 1]);
+  t[9] = addc(t[9], 0);
+}
+
+// reduction part of a CIOS row (m = -t0, r[0] = 1, r[1] = 2^32 - 1), then the
+// one-word shift; bare wide products for m * r[2..7]
+PP_HD void row_red_wide(uint32_t t[10]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  const uint32_t t0 = t[0];
+  const uint32_t m = 0u - t0;
+  uint32_t lo[8], hi[8];
+#pragma unroll
+  for (int j = 2; j < 8; ++j) {
+    const uint64_t p = (uint64_t)m * r[j];
+    lo[j] = (uint32_t)p;
+    hi[j] = (uint32_t)(p >> 32);
+  }
+  (void)sub_cc(0, m);
+  const uint32_t h1 = subc(m, 0);  // hi(m * (2^32 - 1)) = m - (m != 0)
+  (void)add_cc(t0, 0xffffffffu);   // carry out of t0 + m
+  t[1] = addc_cc(t[1], t0);        // lo(m * (2^32 - 1)) = -m = t0
+#pragma unroll
+  for (int j = 2; j < 8; ++j) t[j] = addc_cc(t[j], lo[j]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[2] = add_cc(t[2], h1);
+#pragma unroll
+  for (int j = 2; j < 8; ++j) t[j + 1] = addc_cc(t[j + 1], hi[j]);
+  t[9] = addc(t[9], 0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) t[k] = t[k + 1];
+  t[9] = 0;
+}
+
+// the same reduction part with multiply-add carry chains
+PP_HD void row_red_madc(uint32_t t[10]) {
+  const uint32_t t0 = t[0];
+  const uint32_t m = 0u - t0;
+  (void)sub_cc(0, m);
+  const uint32_t h1 = subc(m, 0);
+  (void)add_cc(t0, 0xffffffffu);
+  t[1] = addc_cc(t[1], t0);
+  t[2] = madloc_cc(m, PP_R2, t[2]);
+  t[3] = madloc_cc(m, PP_R3, t[3]);
+  t[4] = madloc_cc(m, PP_R4, t[4]);
+  t[5] = madloc_cc(m, PP_R5, t[5]);
+  t[6] = madloc_cc(m, PP_R6, t[6]);
+  t[7] = madloc_cc(m, PP_R7, t[7]);
+  t[8] = addc_cc(t[8], 0);
+  t[9] = addc(t[9], 0);
+  t[2] = add_cc(t[2], h1);
+  t[3] = madhic_cc(m, PP_R2, t[3]);
+  t[4] = madhic_cc(m, PP_R3, t[4]);
+  t[5] = madhic_cc(m, PP_R4, t[5]);
+  t[6] = madhic_cc(m, PP_R5, t[6]);
+  t[7] = madhic_cc(m, PP_R6, t[7]);
+  t[8] = madhic_cc(m, PP_R7, t[8]);
+  t[9] = addc(t[9], 0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) t[k] = t[k + 1];
+  t[9] = 0;
+}
+
+// AB: 0 = multiply-add chains, 1 = bare wide products; RED likewise
+template <int AB, int RED>
+PP_HD fr fr_mul_split(const fr &a, const fr &b) {
+  uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (AB) row_ab_wide(t, a.v[i], b.v);
+    else row_ab_madc(t, a.v[i], b.v);
+    if (RED) row_red_wide(t);
+    else row_red_madc(t);
+  }
+  fr_reduce_once(t);
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[i];
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Variant 9: each row's products absorb only the row's own 32-bit word,
+//   s_j = a_i * b_j + t_j   (< 2^64, independent across j),
+// and one add-with-carry chain joins lo(s_j) with hi(s_{j-1}).  The products
+// of a row carry no dependency on each other, and the only addend a wide
+// multiply sees is a zero-extended 32-bit word.
+// ---------------------------------------------------------------------------
+PP_HD void row9_ab(uint32_t t[10], uint32_t ai, const uint32_t b[8]) {
+  uint32_t lo[8], hi[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint64_t s = (uint64_t)ai * b[j] + t[j];
+    lo[j] = (uint32_t)s;
+    hi[j] = (uint32_t)(s >> 32);
+  }
+  t[0] = lo[0];
+  t[1] = add_cc(lo[1], hi[0]);
+#pragma unroll
+  for (int j = 2; j < 8; ++j) t[j] = addc_cc(lo[j], hi[j - 1]);
+  t[8] = addc_cc(t[8], hi[7]);
+  t[9] = addc(t[9], 0);
+}
+
+PP_HD void row9_red(uint32_t t[10]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  const uint32_t t0 = t[0];
+  const uint32_t m = 0u - t0;
+  uint32_t lo[8], hi[8];
+#pragma unroll
+  for (int j = 2; j < 8; ++j) {
+    const uint64_t s = (uint64_t)m * r[j] + t[j];
+    lo[j] = (uint32_t)s;
+    hi[j] = (uint32_t)(s >> 32);
+  }
+  (void)sub_cc(0, m);
+  const uint32_t h1 = subc(m, 0);      // hi(m * (2^32 - 1))
+  (void)add_cc(t0, 0xffffffffu);       // carry out of word 0 (t0 + m)
+  const uint32_t u1 = addc_cc(t[1], t0);  // + lo(m * (2^32 - 1)) = t0
+  const uint32_t u2 = addc_cc(lo[2], h1);
+  const uint32_t u3 = addc_cc(lo[3], hi[2]);
+  const uint32_t u4 = addc_cc(lo[4], hi[3]);
+  const uint32_t u5 = addc_cc(lo[5], hi[4]);
+  const uint32_t u6 = addc_cc(lo[6], hi[5]);
+  const uint32_t u7 = addc_cc(lo[7], hi[6]);
+  const uint32_t u8 = addc_cc(t[8], hi[7]);
+  const uint32_t u9 = addc(t[9], 0);
+  t[0] = u1;
+  t[1] = u2;
+  t[2] = u3;
+  t[3] = u4;
+  t[4] = u5;
+  t[5] = u6;
+  t[6] = u7;
+  t[7] = u8;
+  t[8] = u9;
+  t[9] = 0;
+}
+
+PP_HD fr fr_mul_row9(const fr &a, const fr &b) {
+  uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    row9_ab(t, a.v[i], b.v);
+    row9_red(t);
+  }
+  fr_reduce_once(t);
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[i];
+  return out;
+}
+
 // variant 5: schoolbook product + the same reduction (separated operand scanning)
 PP_HD fr fr_mul_sos(const fr &a, const fr &b) {
   uint32_t t[16];
@@ -553,6 +742,14 @@ PP_HD fr fr_mul(const fr &a, const fr &b) {
   return fr_mul_kara<true>(a, b);
 #elif PP_MUL_VARIANT == 5
   return fr_mul_sos(a, b);
+#elif PP_MUL_VARIANT == 6
+  return fr_mul_split<1, 1>(a, b);
+#elif PP_MUL_VARIANT == 7
+  return fr_mul_split<1, 0>(a, b);
+#elif PP_MUL_VARIANT == 8
+  return fr_mul_split<0, 1>(a, b);
+#elif PP_MUL_VARIANT == 9
+  return fr_mul_row9(a, b);
 #else
   return fr_mul_v<PP_MUL_VARIANT>(a, b);
 #endif

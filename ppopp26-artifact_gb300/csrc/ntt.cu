@@ -118,20 +118,6 @@ __device__ __forceinline__ void dft8(fr x[8], const fr &w1, const fr &w2, const 
   bfly(x[6], x[7]);
 }
 
-struct PassArgs {
-  const fr *in;
-  fr *out;
-  const fr *tw_inner;  // w_R^e, e < R
-  const fr *tw_layer;  // w_{R S}^(c k) at [k][c], or null
-  const fr *diag;      // first pass, NTT_IN_DIAG
-  fr post_scale;
-  uint64_t n_valid;
-  uint32_t lgR, lgT, lgS, lgN;
-  uint32_t first, last, has_post_scale, in_kind, spread;
-  uint32_t P;
-  uint32_t lgRp[4];
-};
-
 __device__ __forceinline__ uint32_t digit_reverse(uint32_t o, uint32_t lgR) {
   uint32_t rem = lgR, p = 0, t = o;
   while (rem > 0) {
@@ -144,13 +130,15 @@ __device__ __forceinline__ uint32_t digit_reverse(uint32_t o, uint32_t lgR) {
   return p;
 }
 
-__global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
-  extern __shared__ uint4 sm[];
+// One tile of one pass.  The block may be wider than the tile needs (batched
+// launches use 256 threads for every job); surplus threads only join the
+// barriers.
+__device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tileid, uint4 *sm) {
   const SmemTile tile{sm, a.lgT};
   const uint32_t R = 1u << a.lgR, T = 1u << a.lgT, E = R << a.lgT;
   const uint32_t nthr = E >> 3;
   const uint32_t tid = threadIdx.x;
-  const uint64_t tileid = blockIdx.x;
+  const bool active = tid < nthr;
 
   uint64_t base = 0, col0 = 0, in_base = 0, out_base = 0;
   uint32_t lgS1 = 0;
@@ -177,7 +165,7 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
   }
 
   // ---- load the tile (coalesced) into shared memory
-  for (uint32_t e = tid; e < E; e += nthr) {
+  for (uint32_t e = tid; active && e < E; e += nthr) {
     uint32_t n, col;
     uint64_t g;
     if (!a.last) {
@@ -218,7 +206,9 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
     while (rem > 0) {
       const uint32_t lgr = rem >= 3 ? 3 : rem;
       const uint32_t lgSj = rem - lgr;
-      if (lgr == 3) {
+      if (!active) {
+        // surplus thread of a wider block: barriers only
+      } else if (lgr == 3) {
         const uint32_t c = d & ((1u << lgSj) - 1), prefix = d >> lgSj;
         const uint32_t pb = (prefix << (lgSj + 3)) + c;
         fr x[8];
@@ -273,7 +263,7 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
   }
 
   // ---- store (coalesced), with the layer twiddle or the final scale
-  for (uint32_t e = tid; e < E; e += nthr) {
+  for (uint32_t e = tid; active && e < E; e += nthr) {
     uint32_t o, col;
     if (a.P == 1) {
       o = e;
@@ -292,6 +282,31 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
           a.P == 1 ? (uint64_t)o : out_base + col + ((uint64_t)o << (a.lgN - a.lgR));
       st_fr(a.out + g, v);
     }
+  }
+}
+
+__global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
+  extern __shared__ uint4 sm[];
+  ntt_tile(a, blockIdx.x, sm);
+}
+
+// Persistent kernel of one batch level: the tiles of every job pass at this
+// level are numbered consecutively (tile_start = prefix sums over the jobs);
+// blocks stride over them.
+__global__ void __launch_bounds__(256, 2)
+    k_ntt_batch_level(const PassArgs *__restrict__ args, const uint64_t *__restrict__ tile_start,
+                      uint32_t count, uint64_t total_tiles) {
+  extern __shared__ uint4 sm[];
+  for (uint64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+    uint32_t lo = 0, hi = count;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (tile_start[mid] <= t) lo = mid;
+      else hi = mid;
+    }
+    const PassArgs a = args[lo];
+    ntt_tile(a, t - tile_start[lo], sm);
+    __syncthreads();  // the next tile reuses the shared memory
   }
 }
 
@@ -593,6 +608,75 @@ void ntt_release_tables() {
   g_pows.clear();
 }
 
+int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inverse,
+                 const NttInputDesc &in, std::vector<PassArgs> &passes,
+                 std::vector<uint64_t> &tiles) {
+  if (lg_m > PP_MAX_LG_N || lg_m < 3) {
+    set_error("batched transform of 2^%u points: supported sizes are 2^3 .. 2^%d", lg_m, PP_MAX_LG_N);
+    return PP_E_UNSUPPORTED;
+  }
+  const uint64_t N = 1ull << lg_m;
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  Plan *plan = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    int st = get_plan(dev, lg_m, inverse, &plan);
+    if (st) return st;
+    if (dev < 64 && !g_attr_set[dev]) {
+      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2048 * (int)sizeof(fr)));
+      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_batch_level,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2048 * (int)sizeof(fr)));
+      g_attr_set[dev] = true;
+    }
+  }
+  if (plan->P > 1 && !work) {
+    set_error("transform of 2^%u points needs a workspace", lg_m);
+    return PP_E_INVAL;
+  }
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.lgN = lg_m;
+  a.P = plan->P;
+  for (uint32_t j = 0; j < plan->P; ++j) a.lgRp[j] = plan->lgR[j];
+  a.diag = in.diag;
+  a.n_valid = in.n_valid ? in.n_valid : N;
+  a.in_kind = (uint32_t)in.kind;
+  a.spread = in.spread;
+  uint32_t acc = 0;
+  for (uint32_t j = 0; j < plan->P; ++j) {
+    acc += plan->lgR[j];
+    a.lgR = plan->lgR[j];
+    a.lgT = plan->lgT[j];
+    a.lgS = lg_m - acc;
+    a.first = j == 0;
+    a.last = j + 1 == plan->P;
+    a.in = j == 0 ? d_in : work;
+    a.out = a.last ? d_out : work;
+    a.tw_inner = plan->tw_inner[j];
+    a.tw_layer = plan->tw_layer[j];
+    a.has_post_scale = a.last && plan->has_post_scale;
+    a.post_scale = plan->post_scale;
+    passes.push_back(a);
+    tiles.push_back(N >> (a.lgR + a.lgT));
+  }
+  return PP_OK;
+}
+
+int ntt_launch_level(const PassArgs *d_args, const uint64_t *d_tile_start, uint32_t count,
+                     uint64_t total_tiles, cudaStream_t stream) {
+  if (!total_tiles) return PP_OK;
+  const uint64_t cap = (uint64_t)device_sm_count() * 2;
+  const unsigned grid = (unsigned)(total_tiles < cap ? total_tiles : cap);
+  k_ntt_batch_level<<<grid, 256, 2048 * sizeof(fr), stream>>>(d_args, d_tile_start, count,
+                                                              total_tiles);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
 int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInputDesc &in,
             cudaStream_t stream) {
   if (lg_m > PP_MAX_LG_N) {
@@ -610,51 +694,21 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
     PP_LAUNCH_CHECK();
     return PP_OK;
   }
-  int dev = 0;
-  PP_CUDA_TRY(cudaGetDevice(&dev));
-  Plan *plan = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    int st = get_plan(dev, lg_m, inverse, &plan);
-    if (st) return st;
-    if (dev < 64 && !g_attr_set[dev]) {
-      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       2048 * (int)sizeof(fr)));
-      g_attr_set[dev] = true;
-    }
-  }
+  uint32_t bits[4], np = 0;
+  ntt_get_split(lg_m, bits, &np);
   fr *work = nullptr;
-  if (plan->P > 1) {
+  if (np > 1) {
     int st = PP_OK;
     work = static_cast<fr *>(workspace_get(N * sizeof(fr), stream, 0, &st));
     if (st) return st;
   }
-  PassArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.lgN = lg_m;
-  a.P = plan->P;
-  for (uint32_t j = 0; j < plan->P; ++j) a.lgRp[j] = plan->lgR[j];
-  a.diag = in.diag;
-  a.n_valid = n_valid;
-  a.in_kind = (uint32_t)in.kind;
-  a.spread = in.spread;
-  uint32_t acc = 0;
-  for (uint32_t j = 0; j < plan->P; ++j) {
-    acc += plan->lgR[j];
-    a.lgR = plan->lgR[j];
-    a.lgT = plan->lgT[j];
-    a.lgS = lg_m - acc;
-    a.first = j == 0;
-    a.last = j + 1 == plan->P;
-    a.in = j == 0 ? d_in : work;
-    a.out = a.last ? d_out : work;
-    a.tw_inner = plan->tw_inner[j];
-    a.tw_layer = plan->tw_layer[j];
-    a.has_post_scale = a.last && plan->has_post_scale;
-    a.post_scale = plan->post_scale;
-    const uint32_t E = 1u << (a.lgR + a.lgT);
-    const uint64_t tiles = N / E;
-    k_ntt_pass<<<(unsigned)tiles, E / 8, E * sizeof(fr), stream>>>(a);
+  std::vector<PassArgs> passes;
+  std::vector<uint64_t> tiles;
+  int st = ntt_describe(d_in, d_out, work, lg_m, inverse, in, passes, tiles);
+  if (st) return st;
+  for (size_t j = 0; j < passes.size(); ++j) {
+    const uint32_t E = 1u << (passes[j].lgR + passes[j].lgT);
+    k_ntt_pass<<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(passes[j]);
     PP_COUNT_LAUNCH();
     PP_LAUNCH_CHECK();
   }

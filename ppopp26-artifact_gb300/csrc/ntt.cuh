@@ -3,9 +3,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "fr.cuh"
 
 namespace pp {
+
+// Everything one launch of the pass kernel needs for one pass of one transform.
+struct PassArgs {
+  const fr *in;
+  fr *out;
+  const fr *tw_inner;  // w_R^e, e < R
+  const fr *tw_layer;  // w_{R S}^(c k) at [k][c], or null
+  const fr *diag;      // first pass, NTT_IN_DIAG
+  fr post_scale;
+  uint64_t n_valid;
+  uint32_t lgR, lgT, lgS, lgN;
+  uint32_t first, last, has_post_scale, in_kind, spread;
+  uint32_t P;
+  uint32_t lgRp[4];
+};
 
 // Host-side field helpers (exact, via the host emulation of fr.cuh).
 fr host_root_of_unity(int lg, bool inverse);  // 7^((r-1)/2^lg) (or its inverse)
@@ -30,6 +47,15 @@ struct NttInputDesc {
 // Returns a PP_* status.  Tables are built and cached on first use per device.
 int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInputDesc &in,
             cudaStream_t stream);
+
+// Per-pass descriptors (and tile counts) of one transform whose passes use
+// `work` (2^lg_m elements) between them; for batch plans.  lg_m >= 3.
+int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inverse,
+                 const NttInputDesc &in, std::vector<PassArgs> &passes,
+                 std::vector<uint64_t> &tiles);
+// One persistent launch over the tiles of `count` job passes (device arrays).
+int ntt_launch_level(const PassArgs *d_args, const uint64_t *d_tile_start, uint32_t count,
+                     uint64_t total_tiles, cudaStream_t stream);
 
 // Builds (or fetches) the cached tables for a transform size (for graph capture
 // the tables must exist before capture starts).

@@ -125,3 +125,15 @@ uint64_t pp_launch_count(void) { return pp::g_launches.load(); }
 int pp_release(void) { return pp::release_all(); }
 
 }  // extern "C"
+
+// Synchronous device -> host copy for callers without their own CUDA binding
+// (e.g. reading serving results from Python).
+extern "C" int pp_copy_to_host(void *h_dst, const void *d_src, uint64_t bytes) {
+  if (!bytes) return PP_OK;
+  if (!h_dst || !d_src) {
+    pp::set_error("pp_copy_to_host: null pointer");
+    return PP_E_INVAL;
+  }
+  PP_CUDA_TRY(cudaMemcpy(h_dst, d_src, bytes, cudaMemcpyDeviceToHost));
+  return PP_OK;
+}

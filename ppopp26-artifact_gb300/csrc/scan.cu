@@ -17,31 +17,11 @@
 // Field arithmetic is exact, so the grouping does not change any result.
 #include "common.cuh"
 #include "ntt.cuh"
+#include "scan.cuh"
 
 #include <mutex>
 
 namespace pp {
-
-constexpr int kScanThreads = 256;
-
-struct ScanGeom {
-  uint64_t n;
-  uint64_t k;        // elements per thread
-  uint64_t threads;  // ceil(n / k)
-  uint32_t blocks;
-};
-
-static ScanGeom scan_geom(uint64_t n) {
-  ScanGeom g;
-  g.n = n;
-  const uint64_t target_threads = (uint64_t)device_sm_count() * 4 * kScanThreads;
-  uint64_t k = (n + target_threads - 1) / target_threads;
-  if (k < 4) k = 4;
-  g.k = k;
-  g.threads = (n + k - 1) / k;
-  g.blocks = (uint32_t)((g.threads + kScanThreads - 1) / kScanThreads);
-  return g;
-}
 
 // ---------------------------------------------------------------- helpers
 // inclusive prefix product over the block (commutative), s: blockDim elements
@@ -84,11 +64,10 @@ __device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb) {
 }
 
 // ------------------------------------------------------------ grand product
-__global__ void __launch_bounds__(kScanThreads) k_gp_local(const fr *__restrict__ in, ScanGeom g,
-                                                            fr *__restrict__ thread_excl,
-                                                            fr *__restrict__ block_total) {
-  __shared__ fr s[kScanThreads];
-  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+__device__ __forceinline__ void gp_local_body(const fr *__restrict__ in, const ScanGeom &g,
+                                              fr *__restrict__ thread_excl,
+                                              fr *__restrict__ block_total, uint32_t blk, fr *s) {
+  const uint64_t gt = blk * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
   fr p = fr_one();
   for (uint64_t i = lo; i < hi; ++i) p = fr_mul(p, ld_fr(in + i));
@@ -96,19 +75,25 @@ __global__ void __launch_bounds__(kScanThreads) k_gp_local(const fr *__restrict_
   // exclusive = inclusive of the previous thread
   const fr excl = threadIdx.x ? s[threadIdx.x - 1] : fr_one();
   if (gt < g.threads) st_fr(thread_excl + gt, excl);
-  if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blockIdx.x, incl);
+  if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blk, incl);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_gp_local(const fr *__restrict__ in, ScanGeom g,
+                                                            fr *__restrict__ thread_excl,
+                                                            fr *__restrict__ block_total) {
+  __shared__ fr s[kScanThreads];
+  gp_local_body(in, g, thread_excl, block_total, blockIdx.x, s);
 }
 
 // out_excl[i] = prod_{j<i} in[j] and/or out_incl[i] = prod_{j<=i} in[j]; either
 // output may be null or alias `in` (each element is read before it is written)
-__global__ void __launch_bounds__(kScanThreads) k_gp_apply(const fr *in, fr *out_excl, fr *out_incl,
-                                                            ScanGeom g,
-                                                            const fr *__restrict__ thread_excl,
-                                                            const fr *__restrict__ block_total) {
-  __shared__ fr s[kScanThreads];
+__device__ __forceinline__ void gp_apply_body(const fr *in, fr *out_excl, fr *out_incl,
+                                              const ScanGeom &g, const fr *__restrict__ thread_excl,
+                                              const fr *__restrict__ block_total, uint32_t blk,
+                                              fr *s) {
   // product of the totals of all earlier blocks
   fr p = fr_one();
-  for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) p = fr_mul(p, ld_fr(block_total + b));
+  for (uint32_t b = threadIdx.x; b < blk; b += blockDim.x) p = fr_mul(p, ld_fr(block_total + b));
   s[threadIdx.x] = p;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -116,7 +101,7 @@ __global__ void __launch_bounds__(kScanThreads) k_gp_apply(const fr *in, fr *out
     __syncthreads();
   }
   const fr block_prefix = s[0];
-  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  const uint64_t gt = blk * (uint64_t)kScanThreads + threadIdx.x;
   if (gt >= g.threads) return;
   fr run = fr_mul(block_prefix, ld_fr(thread_excl + gt));
   const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
@@ -126,6 +111,58 @@ __global__ void __launch_bounds__(kScanThreads) k_gp_apply(const fr *in, fr *out
     run = fr_mul(run, v);
     if (out_incl) st_fr(out_incl + i, run);
   }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_gp_apply(const fr *in, fr *out_excl, fr *out_incl,
+                                                            ScanGeom g,
+                                                            const fr *__restrict__ thread_excl,
+                                                            const fr *__restrict__ block_total) {
+  __shared__ fr s[kScanThreads];
+  gp_apply_body(in, out_excl, out_incl, g, thread_excl, block_total, blockIdx.x, s);
+}
+
+// Batched grand products: the blocks of all jobs are numbered consecutively
+// (block_start = prefix sums); each block finds its job and runs the body.
+__device__ __forceinline__ uint32_t find_job(const uint32_t *__restrict__ start, uint32_t count,
+                                             uint32_t b) {
+  uint32_t lo = 0, hi = count;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_gp_local_batch(const GpBatchJob *__restrict__ jobs,
+                                                                  const uint32_t *__restrict__ start,
+                                                                  uint32_t count) {
+  __shared__ fr s[kScanThreads];
+  const uint32_t j = find_job(start, count, blockIdx.x);
+  const GpBatchJob jb = jobs[j];
+  gp_local_body(jb.in, jb.g, jb.thread_excl, jb.block_total, blockIdx.x - start[j], s);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_gp_apply_batch(const GpBatchJob *__restrict__ jobs,
+                                                                  const uint32_t *__restrict__ start,
+                                                                  uint32_t count) {
+  __shared__ fr s[kScanThreads];
+  const uint32_t j = find_job(start, count, blockIdx.x);
+  const GpBatchJob jb = jobs[j];
+  gp_apply_body(jb.in, jb.out, nullptr, jb.g, jb.thread_excl, jb.block_total, blockIdx.x - start[j],
+                s);
+}
+
+int gp_batch_launch(const GpBatchJob *d_jobs, const uint32_t *d_block_start, uint32_t count,
+                    uint32_t total_blocks, cudaStream_t stream) {
+  if (!total_blocks) return PP_OK;
+  k_gp_local_batch<<<total_blocks, kScanThreads, 0, stream>>>(d_jobs, d_block_start, count);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_gp_apply_batch<<<total_blocks, kScanThreads, 0, stream>>>(d_jobs, d_block_start, count);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
 }
 
 // inclusive suffix product over the block

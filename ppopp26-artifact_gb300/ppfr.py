@@ -15,6 +15,7 @@ import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libppfr.so")
+TUNE_CACHE = os.path.join(HERE, "tune_gb300.json")
 
 _lock = threading.Lock()
 _lib = None
@@ -60,6 +61,14 @@ def lib():
             L.pp_launch_count.restype = ctypes.c_uint64
             L.pp_launch_count.argtypes = []
             _lib = L
+            # radix splits tuned on this GPU model (pp_tune_load ignores another GPU's file)
+            if os.path.exists(TUNE_CACHE) and os.environ.get("PP_NO_TUNE_CACHE") is None:
+                L.pp_tune_load.argtypes = [ctypes.c_char_p]
+                L.pp_tune_load.restype = ctypes.c_int
+                try:
+                    L.pp_tune_load(TUNE_CACHE.encode())
+                except OSError:
+                    pass
         return _lib
 
 
@@ -169,3 +178,208 @@ def launch_count() -> int:
 
 def release() -> None:
     check(lib().pp_release())
+
+
+# ------------------------------------------------------------------ tuning
+def set_split(lg_n: int, bits=None) -> None:
+    """Radix split of 2^lg_n (pass sizes in bits); None restores the default."""
+    L = lib()
+    L.pp_ntt_set_split.argtypes = [ctypes.c_uint32, ctypes.c_void_p]
+    L.pp_ntt_set_split.restype = ctypes.c_int
+    if bits is None:
+        check(L.pp_ntt_set_split(lg_n, None))
+    else:
+        arr = (ctypes.c_uint32 * 5)(*(list(bits) + [0] * (5 - len(bits))))
+        check(L.pp_ntt_set_split(lg_n, ctypes.cast(arr, ctypes.c_void_p)))
+
+
+def get_split(lg_n: int):
+    L = lib()
+    L.pp_ntt_get_split.argtypes = [ctypes.c_uint32, ctypes.c_void_p]
+    L.pp_ntt_get_split.restype = ctypes.c_int
+    arr = (ctypes.c_uint32 * 4)()
+    check(L.pp_ntt_get_split(lg_n, ctypes.cast(arr, ctypes.c_void_p)))
+    return [int(v) for v in arr if v]
+
+
+def autotune(lg_n: int, reps: int = 3):
+    """Time every balanced split of 2^lg_n, keep the fastest; returns (bits, ms)."""
+    L = lib()
+    L.pp_ntt_autotune.argtypes = [ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.pp_ntt_autotune.restype = ctypes.c_int
+    arr = (ctypes.c_uint32 * 4)()
+    ms = ctypes.c_float(0.0)
+    check(L.pp_ntt_autotune(lg_n, reps, ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(ms)))
+    return [int(v) for v in arr if v], float(ms.value)
+
+
+def tune_save(path: str) -> None:
+    L = lib()
+    L.pp_tune_save.argtypes = [ctypes.c_char_p]
+    L.pp_tune_save.restype = ctypes.c_int
+    check(L.pp_tune_save(path.encode()))
+
+
+def tune_load(path: str) -> None:
+    L = lib()
+    L.pp_tune_load.argtypes = [ctypes.c_char_p]
+    L.pp_tune_load.restype = ctypes.c_int
+    check(L.pp_tune_load(path.encode()))
+
+
+# ------------------------------------------------------------------- batch
+JOB_NTT, JOB_INTT, JOB_LDE_COEFFS, JOB_LDE_EVALS, JOB_LDE_SPREAD, JOB_GP = range(6)
+
+
+class _Job(ctypes.Structure):
+    _fields_ = [("d_in", ctypes.c_void_p), ("d_out", ctypes.c_void_p), ("lg_n", ctypes.c_uint32),
+                ("kind", ctypes.c_uint32), ("lam", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Batch:
+    """A batch plan over fixed buffers: jobs are (kind, x, out, lam) tuples."""
+
+    def __init__(self, jobs):
+        L = lib()
+        L.pp_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+        L.pp_batch_create.restype = ctypes.c_int
+        for name in ("pp_batch_run",):
+            getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            getattr(L, name).restype = ctypes.c_int
+        L.pp_batch_capture.argtypes = [ctypes.c_void_p]
+        L.pp_batch_capture.restype = ctypes.c_int
+        L.pp_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.pp_batch_destroy.restype = ctypes.c_int
+        L.pp_batch_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.pp_batch_info.restype = ctypes.c_int
+        self._keep = []
+        arr = (_Job * max(1, len(jobs)))()
+        for i, (kind, x, out, lam) in enumerate(jobs):
+            _ptr(x)
+            _ptr(out)
+            self._keep += [x, out]
+            arr[i] = _Job(x.data_ptr(), out.data_ptr(), _lg(x.shape[0]), kind, lam, 0)
+        self._h = ctypes.c_void_p()
+        check(L.pp_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(jobs), ctypes.byref(self._h)))
+
+    def run(self, stream=None):
+        check(lib().pp_batch_run(self._h, _stream(stream)))
+
+    def capture(self):
+        check(lib().pp_batch_capture(self._h))
+
+    def info(self):
+        la, le = ctypes.c_uint32(), ctypes.c_uint32()
+        ti = ctypes.c_uint64()
+        check(lib().pp_batch_info(self._h, ctypes.byref(la), ctypes.byref(ti), ctypes.byref(le)))
+        return {"launches": la.value, "tiles": ti.value, "levels": le.value}
+
+    def close(self):
+        if self._h:
+            check(lib().pp_batch_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------- serving
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_uint64), ("slots", ctypes.c_uint32), ("min_lg", ctypes.c_uint32),
+                ("max_lg", ctypes.c_uint32), ("lam", ctypes.c_uint32), ("max_queue", ctypes.c_uint32)]
+
+
+class _Bundle(ctypes.Structure):
+    _fields_ = [("lg_n", ctypes.c_uint32), ("lam", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("h_inputs", ctypes.c_void_p), ("h_params", ctypes.c_void_p)]
+
+
+class BundleResult(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("status", ctypes.c_int), ("latency_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("d_lde", ctypes.c_void_p * 3), ("d_z", ctypes.c_void_p),
+                ("d_quotient", ctypes.c_void_p), ("d_evals", ctypes.c_void_p), ("d_w", ctypes.c_void_p * 3),
+                ("d_sigma", ctypes.c_void_p * 3), ("d_params", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("queued", ctypes.c_uint64), ("budget_used", ctypes.c_uint64),
+                ("budget_peak", ctypes.c_uint64), ("admitted_while_busy", ctypes.c_uint64),
+                ("max_concurrent", ctypes.c_uint64), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("bundles_per_s", ctypes.c_double)]
+
+
+def copy_to_host(dptr: int, n_elems: int):
+    """n field elements at a device address -> numpy uint64 (n, 4)."""
+    import numpy as np
+    out = np.empty((n_elems, 4), dtype=np.uint64)
+    L = lib()
+    L.pp_copy_to_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+    L.pp_copy_to_host.restype = ctypes.c_int
+    check(L.pp_copy_to_host(out.ctypes.data, dptr, n_elems * 32))
+    return out
+
+
+class Server:
+    """Continuous-batching server for prover-round bundles (pp_server_*)."""
+
+    def __init__(self, budget_bytes: int, slots: int, min_lg: int, max_lg: int, lam: int = 2, max_queue: int = 0):
+        L = lib()
+        L.pp_server_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        L.pp_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+        L.pp_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]
+        L.pp_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.pp_server_cancel.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.pp_server_get_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.pp_server_reset_stats.argtypes = [ctypes.c_void_p]
+        L.pp_server_destroy.argtypes = [ctypes.c_void_p]
+        for n in ("pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_release",
+                  "pp_server_cancel", "pp_server_get_stats", "pp_server_reset_stats", "pp_server_destroy"):
+            getattr(L, n).restype = ctypes.c_int
+        self.lam = lam
+        cfg = _ServerConfig(budget_bytes, slots, min_lg, max_lg, lam, max_queue)
+        self._h = ctypes.c_void_p()
+        check(L.pp_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    def submit(self, lg_n: int, seed: int, h_inputs=None, h_params=None) -> int:
+        b = _Bundle(lg_n, self.lam, seed & (2**64 - 1),
+                    None if h_inputs is None else h_inputs.data_ptr(),
+                    None if h_params is None else h_params.data_ptr())
+        t = ctypes.c_uint64()
+        check(lib().pp_server_submit(self._h, ctypes.byref(b), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> BundleResult:
+        r = BundleResult()
+        check(lib().pp_server_wait(self._h, ticket, timeout_ms, ctypes.byref(r)))
+        return r
+
+    def wait_status(self, ticket: int, timeout_ms: int) -> int:
+        return lib().pp_server_wait(self._h, ticket, timeout_ms, None)
+
+    def release(self, ticket: int) -> None:
+        check(lib().pp_server_release(self._h, ticket))
+
+    def cancel(self, ticket: int) -> int:
+        return lib().pp_server_cancel(self._h, ticket)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().pp_server_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        check(lib().pp_server_reset_stats(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            check(lib().pp_server_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
