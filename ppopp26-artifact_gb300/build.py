@@ -27,7 +27,7 @@ COMPAT_DRIVER = os.path.join(HERE, "pp_compat_driver")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Montgomery multiply formulation (csrc/fr.cuh); overridable for experiments
-MUL_VARIANT = os.environ.get("PP_MUL_VARIANT", "2")
+MUL_VARIANT = os.environ.get("PP_MUL_VARIANT", "9")
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-DPP_MUL_VARIANT=" + MUL_VARIANT,
               "-I" + os.path.join(ROOT, "include")]
 

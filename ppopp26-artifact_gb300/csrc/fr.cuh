@@ -726,6 +726,127 @@ PP_HD fr fr_mul_row9(const fr &a, const fr &b) {
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// Variant 10: variant 9's row structure inside a one-level Karatsuba product
+// (3 products of 4x4 limbs = 48 wide products instead of 64) followed by a
+// word-serial reduction of the 512-bit product with the same row structure.
+// ---------------------------------------------------------------------------
+// r[0..8) = a[0..4) * b[0..4), rows of independent products + one chain
+PP_HD void mul4_rows(uint32_t r[8], const uint32_t a[4], const uint32_t b[4]) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) r[k] = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    uint32_t lo[4], hi[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint64_t s = (uint64_t)a[i] * b[j] + r[i + j];
+      lo[j] = (uint32_t)s;
+      hi[j] = (uint32_t)(s >> 32);
+    }
+    r[i] = lo[0];
+    r[i + 1] = add_cc(lo[1], hi[0]);
+    r[i + 2] = addc_cc(lo[2], hi[1]);
+    r[i + 3] = addc_cc(lo[3], hi[2]);
+    r[i + 4] = addc(hi[3], 0);
+  }
+}
+
+PP_HD void mul8_kara_rows(uint32_t r[16], const uint32_t a[8], const uint32_t b[8]) {
+  uint32_t sa[4], sb[4];
+  sa[0] = add_cc(a[0], a[4]);
+  sa[1] = addc_cc(a[1], a[5]);
+  sa[2] = addc_cc(a[2], a[6]);
+  sa[3] = addc_cc(a[3], a[7]);
+  const uint32_t ca = addc(0, 0);
+  sb[0] = add_cc(b[0], b[4]);
+  sb[1] = addc_cc(b[1], b[5]);
+  sb[2] = addc_cc(b[2], b[6]);
+  sb[3] = addc_cc(b[3], b[7]);
+  const uint32_t cb = addc(0, 0);
+  uint32_t z0[8], z2[8], z1[8];
+  mul4_rows(z0, a, b);
+  mul4_rows(z2, a + 4, b + 4);
+  mul4_rows(z1, sa, sb);
+  // z1 += (ca * sb + cb * sa) << 128, top word z1t
+  const uint32_t ma = 0u - ca, mb = 0u - cb;
+  z1[4] = add_cc(z1[4], sb[0] & ma);
+  z1[5] = addc_cc(z1[5], sb[1] & ma);
+  z1[6] = addc_cc(z1[6], sb[2] & ma);
+  z1[7] = addc_cc(z1[7], sb[3] & ma);
+  uint32_t z1t = addc(ca & cb, 0);
+  z1[4] = add_cc(z1[4], sa[0] & mb);
+  z1[5] = addc_cc(z1[5], sa[1] & mb);
+  z1[6] = addc_cc(z1[6], sa[2] & mb);
+  z1[7] = addc_cc(z1[7], sa[3] & mb);
+  z1t = addc(z1t, 0);
+  // z1 -= z0 + z2 (non-negative middle term a0*b1 + a1*b0)
+  z1[0] = sub_cc(z1[0], z0[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) z1[i] = subc_cc(z1[i], z0[i]);
+  z1t = subc(z1t, 0);
+  z1[0] = sub_cc(z1[0], z2[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) z1[i] = subc_cc(z1[i], z2[i]);
+  z1t = subc(z1t, 0);
+  // r = z0 + z1 << 128 + z2 << 256
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r[i] = z0[i];
+  r[4] = add_cc(z0[4], z1[0]);
+  r[5] = addc_cc(z0[5], z1[1]);
+  r[6] = addc_cc(z0[6], z1[2]);
+  r[7] = addc_cc(z0[7], z1[3]);
+  r[8] = addc_cc(z2[0], z1[4]);
+  r[9] = addc_cc(z2[1], z1[5]);
+  r[10] = addc_cc(z2[2], z1[6]);
+  r[11] = addc_cc(z2[3], z1[7]);
+  r[12] = addc_cc(z2[4], z1t);
+  r[13] = addc_cc(z2[5], 0);
+  r[14] = addc_cc(z2[6], 0);
+  r[15] = addc(z2[7], 0);
+}
+
+// word-serial Montgomery reduction of t[0..16) with variant 9's rows; the
+// carry out of round i's top word (i + 8) is added at round i+1's top word
+PP_HD fr mont_redc16_rows(uint32_t t[16]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  uint32_t hc = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t t0 = t[i];
+    const uint32_t m = 0u - t0;
+    uint32_t lo[8], hi[8];
+#pragma unroll
+    for (int j = 2; j < 8; ++j) {
+      const uint64_t s = (uint64_t)m * r[j] + t[i + j];
+      lo[j] = (uint32_t)s;
+      hi[j] = (uint32_t)(s >> 32);
+    }
+    (void)sub_cc(0, m);
+    const uint32_t h1 = subc(m, 0);
+    (void)add_cc(t0, 0xffffffffu);
+    t[i + 1] = addc_cc(t[i + 1], t0);
+    t[i + 2] = addc_cc(lo[2], h1);
+#pragma unroll
+    for (int j = 3; j < 8; ++j) t[i + j] = addc_cc(lo[j], hi[j - 1]);
+    t[i + 8] = addc_cc(t[i + 8], hi[7]);
+    const uint32_t c1 = addc(0, 0);
+    t[i + 8] = add_cc(t[i + 8], hc);
+    hc = addc(c1, 0);
+  }
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[8 + i];
+  fr_reduce_once(out.v);
+  return out;
+}
+
+PP_HD fr fr_mul_kara_rows(const fr &a, const fr &b) {
+  uint32_t t[16];
+  mul8_kara_rows(t, a.v, b.v);
+  return mont_redc16_rows(t);
+}
+
 // variant 5: schoolbook product + the same reduction (separated operand scanning)
 PP_HD fr fr_mul_sos(const fr &a, const fr &b) {
   uint32_t t[16];
@@ -750,6 +871,8 @@ PP_HD fr fr_mul(const fr &a, const fr &b) {
   return fr_mul_split<0, 1>(a, b);
 #elif PP_MUL_VARIANT == 9
   return fr_mul_row9(a, b);
+#elif PP_MUL_VARIANT == 10
+  return fr_mul_kara_rows(a, b);
 #else
   return fr_mul_v<PP_MUL_VARIANT>(a, b);
 #endif
@@ -793,6 +916,85 @@ PP_HD fr fr_inv(const fr &a) {
     }
   }
   return acc;
+}
+
+// ---------------------------------------------------------------------------
+// Inverse by the binary extended Euclidean algorithm (Knuth TAOCP vol. 2,
+// 4.5.2; Menezes et al., Handbook of Applied Cryptography, Alg. 14.61 for an
+// odd modulus): a few hundred shift / subtract steps on 8-limb words instead
+// of the ~320 dependent Montgomery multiplies of a Fermat exponentiation.
+// Variable time (fine for public prover data).  Input and output are in
+// Montgomery form: the plain inverse y of the representative a*R is
+// R^-1 a^-1, so the result is y * R^3 * R^-1 = (a^-1) R.  0 maps to 0.
+// ---------------------------------------------------------------------------
+PP_HD bool lt_words(const uint32_t a[8], const uint32_t b[8]) {
+  for (int i = 7; i >= 0; --i)
+    if (a[i] != b[i]) return a[i] < b[i];
+  return false;
+}
+PP_HD bool is_one_words(const uint32_t a[8]) {
+  return a[0] == 1 && (a[1] | a[2] | a[3] | a[4] | a[5] | a[6] | a[7]) == 0;
+}
+// x = x / 2 (mod r) for x < r
+PP_HD void half_mod(uint32_t x[8]) {
+  const uint32_t odd = 0u - (x[0] & 1u);
+  uint32_t c;
+  x[0] = add_cc(x[0], PP_R0 & odd);
+  x[1] = addc_cc(x[1], PP_R1 & odd);
+  x[2] = addc_cc(x[2], PP_R2 & odd);
+  x[3] = addc_cc(x[3], PP_R3 & odd);
+  x[4] = addc_cc(x[4], PP_R4 & odd);
+  x[5] = addc_cc(x[5], PP_R5 & odd);
+  x[6] = addc_cc(x[6], PP_R6 & odd);
+  x[7] = addc_cc(x[7], PP_R7 & odd);
+  c = addc(0, 0);
+#pragma unroll
+  for (int i = 0; i < 7; ++i) x[i] = (x[i] >> 1) | (x[i + 1] << 31);
+  x[7] = (x[7] >> 1) | (c << 31);
+}
+PP_HD void shr1_words(uint32_t x[8]) {
+#pragma unroll
+  for (int i = 0; i < 7; ++i) x[i] = (x[i] >> 1) | (x[i + 1] << 31);
+  x[7] >>= 1;
+}
+PP_HD void sub_words(uint32_t a[8], const uint32_t b[8]) {
+  a[0] = sub_cc(a[0], b[0]);
+#pragma unroll
+  for (int i = 1; i < 7; ++i) a[i] = subc_cc(a[i], b[i]);
+  a[7] = subc(a[7], b[7]);
+}
+
+PP_HD fr fr_inv_binary(const fr &a) {
+  if (fr_is_zero(a)) return fr_zero();
+  uint32_t u[8], v[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  fr x1 = fr_zero(), x2 = fr_zero();
+  x1.v[0] = 1;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) u[i] = a.v[i];
+  // at most ~2 * 256 halvings and 256 subtractions for canonical input; the
+  // bounds only guard against non-canonical input (u or v reaching 0)
+  for (int guard = 0; guard < 1024 && !is_one_words(u) && !is_one_words(v); ++guard) {
+    for (int k = 0; k < 256 && !(u[0] & 1u); ++k) {
+      shr1_words(u);
+      half_mod(x1.v);
+    }
+    for (int k = 0; k < 256 && !(v[0] & 1u); ++k) {
+      shr1_words(v);
+      half_mod(x2.v);
+    }
+    if (!lt_words(u, v)) {
+      sub_words(u, v);
+      x1 = fr_sub(x1, x2);
+    } else {
+      sub_words(v, u);
+      x2 = fr_sub(x2, x1);
+    }
+  }
+  const fr y = is_one_words(u) ? x1 : x2;
+  // R^3 mod r
+  const fr r3 = {{0x439b73afu, 0xc62c1807u, 0x8cf06990u, 0x1b3e0d18u,
+                  0xc7b5f418u, 0x73d13c71u, 0xc8db33e9u, 0x6e2a5bb9u}};
+  return fr_mul(y, r3);
 }
 
 }  // namespace pp

@@ -8,9 +8,9 @@
 //  1. every thread folds a contiguous chunk of K elements into one summary
 //     (a product for the grand product; an affine map S_start = a + b*S_end for
 //     the backward recurrence S_i = p_i + m*S_{i+1} behind both evaluation,
-//     m = x, and division, m = -c); a block-wide Hillis-Steele scan over the
+//     m = x, and division, m = -c); a block-wide work-efficient scan over the
 //     256 thread summaries in shared memory gives every thread its in-block
-//     carry and the block its summary;
+//     carry and the block its summary (evaluation needs only the summary);
 //  2. every block folds the summaries of the blocks before it (grand product)
 //     or after it (division) and each thread replays its chunk with the exact
 //     carry; evaluation composes all block maps in one block.
@@ -24,43 +24,97 @@
 namespace pp {
 
 // ---------------------------------------------------------------- helpers
-// inclusive prefix product over the block (commutative), s: blockDim elements
+// Block scans are work-efficient (Blelloch, "Prefix sums and their
+// applications", 1990): an up-sweep and a down-sweep over a balanced tree,
+// 2(n-1) combines for n = blockDim.x (a power of two) instead of the n log n
+// of a Hillis-Steele scan -- each combine here is one or two field multiplies.
+
+// inclusive prefix product over the block (commutative); afterwards s[t]
+// holds thread t's inclusive product, which is also returned
 __device__ fr block_prefix_product(fr v, fr *s) {
   const int t = threadIdx.x, n = blockDim.x;
   s[t] = v;
   __syncthreads();
-  for (int o = 1; o < n; o <<= 1) {
-    fr nv = v;
-    if (t >= o) nv = fr_mul(s[t - o], v);
-    __syncthreads();
-    s[t] = nv;
-    v = nv;
+  for (int d = 1; d < n; d <<= 1) {
+    const int idx = (t + 1) * 2 * d - 1;
+    if (idx < n) s[idx] = fr_mul(s[idx - d], s[idx]);
     __syncthreads();
   }
-  return v;
-}
-
-// inclusive suffix composition of affine maps f_t(x) = a_t + b_t x over the
-// block: afterwards (a, b) = f_t o f_{t+1} o ... o f_{n-1}
-__device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb) {
-  const int t = threadIdx.x, n = blockDim.x;
-  sa[t] = a;
-  sb[t] = b;
+  if (t == 0) s[n - 1] = fr_one();
   __syncthreads();
-  for (int o = 1; o < n; o <<= 1) {
-    fr na = a, nb = b;
-    if (t + o < n) {
-      const fr a2 = sa[t + o], b2 = sb[t + o];
-      na = fr_add(a, fr_mul(b, a2));
-      nb = fr_mul(b, b2);
+  for (int d = n >> 1; d >= 1; d >>= 1) {
+    const int idx = (t + 1) * 2 * d - 1;
+    if (idx < n) {
+      const fr left = s[idx - d];
+      s[idx - d] = s[idx];
+      s[idx] = fr_mul(s[idx], left);
     }
     __syncthreads();
-    sa[t] = na;
-    sb[t] = nb;
-    a = na;
-    b = nb;
+  }
+  const fr incl = fr_mul(s[t], v);
+  __syncthreads();
+  s[t] = incl;
+  __syncthreads();
+  return incl;
+}
+
+// Suffix composition of affine maps f_t(x) = a_t + b_t x over the block.
+// Afterwards (a, b) = F_t = f_t o f_{t+1} o ... o f_{n-1} and, when `all`,
+// (sa[t], sb[t]) = F_t for every t; without `all` only F_0 is produced (in
+// thread 0's (a, b) and sa[0], sb[0]).  Scanned in reversed order u = n-1-t,
+// where the running composition is G_u = g_u o G_{u-1}.
+__device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb, bool all = true) {
+  const int t = threadIdx.x, n = blockDim.x;
+  const int u = n - 1 - t;
+  sa[u] = a;
+  sb[u] = b;
+  __syncthreads();
+  // combine(left = earlier in u, right = later in u) = right o left
+  for (int d = 1; d < n; d <<= 1) {
+    const int idx = (t + 1) * 2 * d - 1;
+    if (idx < n) {
+      const fr la = sa[idx - d], lb = sb[idx - d], ra = sa[idx], rb = sb[idx];
+      sa[idx] = fr_add(ra, fr_mul(rb, la));
+      sb[idx] = fr_mul(rb, lb);
+    }
     __syncthreads();
   }
+  if (!all) {
+    // sa[n-1], sb[n-1] = G_{n-1} = F_0
+    if (t == 0) {
+      a = sa[n - 1];
+      b = sb[n - 1];
+      sa[0] = a;
+      sb[0] = b;
+    }
+    __syncthreads();
+    return;
+  }
+  if (t == 0) {
+    sa[n - 1] = fr_zero();
+    sb[n - 1] = fr_one();
+  }
+  __syncthreads();
+  for (int d = n >> 1; d >= 1; d >>= 1) {
+    const int idx = (t + 1) * 2 * d - 1;
+    if (idx < n) {
+      const fr la = sa[idx - d], lb = sb[idx - d], pa = sa[idx], pb = sb[idx];
+      sa[idx - d] = pa;
+      sb[idx - d] = pb;
+      sa[idx] = fr_add(la, fr_mul(lb, pa));  // left o P
+      sb[idx] = fr_mul(lb, pb);
+    }
+    __syncthreads();
+  }
+  // exclusive E_u in (sa[u], sb[u]); inclusive G_u = g_u o E_u = F_t
+  const fr ea = sa[u], eb = sb[u];
+  const fr ia = fr_add(a, fr_mul(b, ea)), ib = fr_mul(b, eb);
+  __syncthreads();
+  sa[t] = ia;
+  sb[t] = ib;
+  a = ia;
+  b = ib;
+  __syncthreads();
 }
 
 // ------------------------------------------------------------ grand product
@@ -226,7 +280,7 @@ __global__ void __launch_bounds__(kScanThreads) k_perm_local(const PermArgs a, S
   const fr U = block_suffix_product(D, s2);  // s2[t] = D_t..D_last
   (void)Q;
   (void)U;
-  if (threadIdx.x == 0) s_inv = fr_inv(s1[blockDim.x - 1]);
+  if (threadIdx.x == 0) s_inv = fr_inv_binary(s1[blockDim.x - 1]);
   __syncthreads();
   fr acc = s_inv;
   if (threadIdx.x > 0) acc = fr_mul(acc, s1[threadIdx.x - 1]);
@@ -276,7 +330,7 @@ __global__ void __launch_bounds__(kScanThreads) k_affine_local(const fr *__restr
   const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
   fr a, b;
   chunk_map(p, lo, hi, m, a, b);
-  block_affine_suffix(a, b, sa, sb);
+  block_affine_suffix(a, b, sa, sb, thread_a != nullptr);
   if (thread_a && gt < g.threads) {
     const bool last = threadIdx.x == blockDim.x - 1;
     st_fr(thread_a + gt, last ? fr_zero() : sa[threadIdx.x + 1]);
@@ -303,7 +357,7 @@ __device__ void compose_blocks(const fr *block_a, const fr *block_b, uint32_t fi
     a = fr_add(ai, fr_mul(bi, a));
     b = fr_mul(bi, b);
   }
-  block_affine_suffix(a, b, sa, sb);
+  block_affine_suffix(a, b, sa, sb, false);
   A = sa[0];
   B = sb[0];
 }

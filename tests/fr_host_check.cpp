@@ -40,11 +40,11 @@ int main(int argc, char **argv) {
     fr m0 = pp::fr_mul_v<0>(x, y), m1 = pp::fr_mul_v<1>(x, y), m2 = pp::fr_mul_w(x, y);
     fr m3 = pp::fr_mul_kara<false>(x, y), m4 = pp::fr_mul_kara<true>(x, y), m5 = pp::fr_mul_sos(x, y);
     fr m6 = pp::fr_mul_split<1, 1>(x, y), m7 = pp::fr_mul_split<1, 0>(x, y), m8 = pp::fr_mul_split<0, 1>(x, y);
-    fr m9 = pp::fr_mul_row9(x, y);
+    fr m9 = pp::fr_mul_row9(x, y), m10 = pp::fr_mul_kara_rows(x, y);
     if (std::memcmp(m0.v, want, 32) || std::memcmp(m1.v, want, 32) || std::memcmp(m2.v, want, 32) ||
         std::memcmp(m3.v, want, 32) || std::memcmp(m4.v, want, 32) || std::memcmp(m5.v, want, 32) ||
         std::memcmp(m6.v, want, 32) || std::memcmp(m7.v, want, 32) || std::memcmp(m8.v, want, 32) ||
-        std::memcmp(m9.v, want, 32)) {
+        std::memcmp(m9.v, want, 32) || std::memcmp(m10.v, want, 32)) {
       if (bad++ < 5) std::printf("mul mismatch at %llu\n", (unsigned long long)i);
     }
     or_fr_add(a + 4 * i, b + 4 * i, want);
@@ -62,6 +62,10 @@ int main(int argc, char **argv) {
       fr v = pp::fr_inv(x);
       if (std::memcmp(v.v, want, 32)) {
         if (bad++ < 5) std::printf("inv mismatch at %llu\n", (unsigned long long)i);
+      }
+      fr vb = pp::fr_inv_binary(x);
+      if (std::memcmp(vb.v, want, 32)) {
+        if (bad++ < 5) std::printf("binary inv mismatch at %llu\n", (unsigned long long)i);
       }
       uint64_t e[4] = {i * 7919 + 3, 0, 0, 0};
       or_fr_pow(a + 4 * i, e, want);
