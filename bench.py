@@ -326,8 +326,12 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "int", "kernel": "k_ntt_pass", "achieved": round(achieved_int, 3),
                      "peak": round(int_peak, 3), "unit": "Tinstr/s", "frac": round(achieved_int / int_peak, 4),
                      "traffic": traffic,
+                     "mixed_rate_ceiling": round(int_peak * 2 / 3, 3),
+                     "frac_of_mixed_rate_ceiling": round(achieved_int / (int_peak * 2 / 3), 4),
                      "note": "algorithmic (N/2)lgN Montgomery multiplies x 256 32-bit multiply instructions; "
-                             "peak = SMs x 64 multiply lanes/clk x median SM clock under load"},
+                             "peak = SMs x 64 multiply lanes/clk x median SM clock under load (the low-half "
+                             "rate); half of the 256 are high halves at half that rate, so 2/3 of peak is "
+                             "the ceiling for any multiply built from them"},
         "roofline_hbm": {"bound": "hbm", "achieved": round(achieved_hbm, 2), "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": round(achieved_hbm / peaks.get("hbm_gbs", 6800.0), 4),
                          "peak_kind": peak_kind},

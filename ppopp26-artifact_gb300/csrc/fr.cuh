@@ -727,6 +727,31 @@ PP_HD fr fr_mul_row9(const fr &a, const fr &b) {
 }
 
 // ---------------------------------------------------------------------------
+// Variants 11-13: variant 9's rows for part of the multiply and bare wide
+// products with two add chains for the rest.  A wide multiply with an addend
+// holds the integer-multiply pipe ~1.4x longer than a bare one, and the second
+// add chain runs on the ALU pipe, so the mix trades multiply-pipe cycles for
+// ALU cycles.  AB / RED choose the rows: 0 = variant 9, 1 = bare products,
+// 2 = bare on odd rows only.  Both row forms keep the same t[0..10) invariant.
+// ---------------------------------------------------------------------------
+template <int AB, int RED>
+PP_HD fr fr_mul_mix(const fr &a, const fr &b) {
+  uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (AB == 1 || (AB == 2 && (i & 1))) row_ab_wide(t, a.v[i], b.v);
+    else row9_ab(t, a.v[i], b.v);
+    if (RED == 1 || (RED == 2 && (i & 1))) row_red_wide(t);
+    else row9_red(t);
+  }
+  fr_reduce_once(t);
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = t[i];
+  return out;
+}
+
+// ---------------------------------------------------------------------------
 // Variant 10: variant 9's row structure inside a one-level Karatsuba product
 // (3 products of 4x4 limbs = 48 wide products instead of 64) followed by a
 // word-serial reduction of the 512-bit product with the same row structure.
@@ -873,6 +898,12 @@ PP_HD fr fr_mul(const fr &a, const fr &b) {
   return fr_mul_row9(a, b);
 #elif PP_MUL_VARIANT == 10
   return fr_mul_kara_rows(a, b);
+#elif PP_MUL_VARIANT == 11
+  return fr_mul_mix<0, 1>(a, b);
+#elif PP_MUL_VARIANT == 12
+  return fr_mul_mix<1, 0>(a, b);
+#elif PP_MUL_VARIANT == 13
+  return fr_mul_mix<0, 2>(a, b);
 #else
   return fr_mul_v<PP_MUL_VARIANT>(a, b);
 #endif

@@ -41,10 +41,12 @@ int main(int argc, char **argv) {
     fr m3 = pp::fr_mul_kara<false>(x, y), m4 = pp::fr_mul_kara<true>(x, y), m5 = pp::fr_mul_sos(x, y);
     fr m6 = pp::fr_mul_split<1, 1>(x, y), m7 = pp::fr_mul_split<1, 0>(x, y), m8 = pp::fr_mul_split<0, 1>(x, y);
     fr m9 = pp::fr_mul_row9(x, y), m10 = pp::fr_mul_kara_rows(x, y);
+    fr m11 = pp::fr_mul_mix<0, 1>(x, y), m12 = pp::fr_mul_mix<1, 0>(x, y), m13 = pp::fr_mul_mix<0, 2>(x, y);
     if (std::memcmp(m0.v, want, 32) || std::memcmp(m1.v, want, 32) || std::memcmp(m2.v, want, 32) ||
         std::memcmp(m3.v, want, 32) || std::memcmp(m4.v, want, 32) || std::memcmp(m5.v, want, 32) ||
         std::memcmp(m6.v, want, 32) || std::memcmp(m7.v, want, 32) || std::memcmp(m8.v, want, 32) ||
-        std::memcmp(m9.v, want, 32) || std::memcmp(m10.v, want, 32)) {
+        std::memcmp(m9.v, want, 32) || std::memcmp(m10.v, want, 32) || std::memcmp(m11.v, want, 32) ||
+        std::memcmp(m12.v, want, 32) || std::memcmp(m13.v, want, 32)) {
       if (bad++ < 5) std::printf("mul mismatch at %llu\n", (unsigned long long)i);
     }
     or_fr_add(a + 4 * i, b + 4 * i, want);
