@@ -6,8 +6,11 @@ A step is one forward NTT of 2^24 seeded random canonical Fr elements
 (512 MiB, larger than the 129 MB L2, so no flush is needed between steps).
 `value` is device throughput with the input resident in HBM (Melem/s =
 2^24 * K * n_gpus / max-over-ranks time); `e2e` is the same metric through the
-C ABI with host buffers: each step copies the input from pinned host memory,
-transforms it and copies the result back.  `roofline` is the integer-multiply
+C ABI with pinned host buffers in and out.  Three forms are timed: pp_ntt_host
+(the first pass reads the host input over NVLink-C2C and the last pass writes
+the host output), copies + transform one step at a time, and copies of
+neighbouring steps overlapped with the transform on three streams.  The
+headline is the faster of the first and last.  `roofline` is the integer-multiply
 pipe bound of the transform kernel; `roofline_hbm` its HBM view.  Extra
 operators (INTT, LDE, grand products, evaluation, division) are timed after
 the headline and reported under `ops`.
@@ -282,16 +285,29 @@ def run_ours(args, rank, world, local):
 
     e2e_stream(2)
     e2e_ms = e2e_stream(e2e_steps)
+    # host-resident form (pp_ntt_host): the first pass reads the pinned input
+    # over NVLink-C2C and the last pass writes the pinned output; no copies
+    hout_d = torch.empty_like(hin, pin_memory=True)
+    e2e_direct_ms = time_device(lambda: ppfr.ntt_host(hin, out=hout_d), e2e_steps, 1, torch)
     clk = clocks.stop()
     # max over ranks
-    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps, e2e_serial_ms / e2e_steps * args.steps],
-                     dtype=torch.float64, device="cuda")
+    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps, e2e_serial_ms / e2e_steps * args.steps,
+                      e2e_direct_ms / e2e_steps * args.steps], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms_norm, e2e_serial_norm = float(t[0]), float(t[1]), float(t[2])
+    ms, e2e_ms_norm, e2e_serial_norm, e2e_direct_norm = (float(v) for v in t)
     value = N * args.steps * world / (ms / 1e3) / 1e6
-    e2e_value = N * args.steps * world / (e2e_ms_norm / 1e3) / 1e6
+    e2e_stream_value = N * args.steps * world / (e2e_ms_norm / 1e3) / 1e6
     e2e_serial_value = N * args.steps * world / (e2e_serial_norm / 1e3) / 1e6
+    e2e_direct_value = N * args.steps * world / (e2e_direct_norm / 1e3) / 1e6
+    same = torch.equal(hout_d, hout)  # both forms transformed the same input
+    if e2e_direct_value >= e2e_stream_value:
+        e2e_value, e2e_form = e2e_direct_value, (
+            "host-resident: pp_ntt_host on pinned host buffers, pass 1 reads the input over "
+            "NVLink-C2C and the last pass writes the output; one call per step, no overlap between steps")
+    else:
+        e2e_value, e2e_form = e2e_stream_value, (
+            "streamed: H2D / NTT / D2H of neighbouring steps overlap on 3 streams")
 
     ops = {}
     if not args.no_ops and rank == 0:
@@ -319,9 +335,10 @@ def run_ours(args, rank, world, local):
         "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N,
                    "l2_flush": "not needed: 512 MiB input > 129 MB L2", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Melem/s", "h2d_bytes_per_step": 32 * N,
-                "d2h_bytes_per_step": 32 * N, "steps": e2e_steps,
-                "form": "streamed: H2D / NTT / D2H of neighbouring steps overlap on 3 streams",
-                "serial_value": round(e2e_serial_value, 3)},
+                "d2h_bytes_per_step": 32 * N, "steps": e2e_steps, "form": e2e_form,
+                "host_resident_value": round(e2e_direct_value, 3),
+                "streamed_value": round(e2e_stream_value, 3),
+                "serial_value": round(e2e_serial_value, 3), "forms_agree": bool(same)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "k_ntt_pass", "achieved": round(achieved_int, 3),
                      "peak": round(int_peak, 3), "unit": "Tinstr/s", "frac": round(achieved_int / int_peak, 4),
@@ -384,9 +401,47 @@ def secondary_ops(pp, torch):
     zz = ppfr.empty(n)
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
     del w, s, p
+    constraint_bench(pp, torch, rate, res)
     res["batched"] = batched_bench(pp, torch)
     res["serving"] = serving_bench(pp, torch)
     return res
+
+
+def constraint_bench(pp, torch, rate, res):
+    """Quotient-constraint operators over 2^22 extended-domain points (the 8x
+    LDE of a 2^19-row circuit), with the integer-pipe fraction of each:
+    18 Montgomery multiplies per point for the fused permutation terms and 104
+    for the gate terms at sbox_alpha = 5, 256 multiply instructions each."""
+    ppfr = pp.ppfr
+    n = 1 << 22
+    sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s at the maximum SM clock
+
+    def vec(i):
+        return ppfr.random_fr(n, 0xC0 + i)
+
+    def scal(i):
+        return ppfr.random_fr(1, 0xD0 + i)
+
+    w = [vec(j) for j in range(4)]
+    sig = [vec(4 + j) for j in range(4)]
+    x, z, zn, mod, l1 = vec(8), vec(9), vec(10), vec(11), vec(12)
+    ks = [scal(j) for j in range(3)]
+    al, be, ga, one = scal(3), scal(4), scal(5), scal(6)
+    out = ppfr.empty(n)
+    name = "quotient_permutation_2^22"
+    rate(name, lambda: ppfr.quotient_permutation(x, w, z, zn, sig, mod, l1, al, be, ga, ks, one,
+                                                 out=out), n, 5)
+    res[name].update({"MM_per_point": 18, "bytes_per_point": 448})
+    del w, sig, x, z, zn, mod, l1
+    V = {k: vec(20 + i) for i, k in enumerate(ppfr.GATE_VECTORS)}
+    S = {k: scal(20 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
+    name = "gate_constraint_2^22"
+    rate(name, lambda: ppfr.gate_constraint(V, S, 5, out=out), n, 3)
+    res[name].update({"MM_per_point": 104, "bytes_per_point": 736})
+    for k, mm in (("quotient_permutation_2^22", 18), ("gate_constraint_2^22", 104)):
+        pts = res[k]["Melem_per_s"] * 1e6
+        res[k]["int_frac_of_nominal_peak"] = round(pts * mm * 256 / peak, 4)
 
 
 def batched_bench(pp, torch):

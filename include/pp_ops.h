@@ -86,6 +86,23 @@ int pp_tune_load(const char *path);
 int pp_lde(const void *d_in, void *d_out, uint32_t lg_n, uint32_t lambda, uint32_t mode,
            void *stream);
 
+/* ------------------------------------------------- host-resident forms ---
+ * The same transforms with input and output in page-locked host memory
+ * (cudaHostAlloc / cudaMallocHost / cudaHostRegister).  The first pass reads
+ * the input from host memory and the last pass writes the output there
+ * (NVLink-C2C on Grace hosts); the intermediate passes use an HBM workspace.
+ * Asynchronous on the stream: synchronise it before reading h_out.  A buffer
+ * that is not page-locked host memory is refused with PP_E_INVAL before any
+ * kernel is launched.  h_in == h_out is allowed for pp_ntt_host.
+ * Replaces the reference's host-resident drivers our_ntt (ntt.cu:979-1037,
+ * in place on a pinned host buffer, with run_first_ntt_pass :801 and
+ * run_second_ntt_pass_async_scatter :861 staging chunks through the device
+ * and permuting on the CPU) and our_lde (lde.cu:1267-1365, host input
+ * lde.cu:1033 run_first_lde_pass, host output). */
+int pp_ntt_host(const void *h_in, void *h_out, uint32_t lg_n, int inverse, void *stream);
+int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda, uint32_t mode,
+                void *stream);
+
 /* ------------------------------------------------------- grand product ---
  * Exclusive prefix product in place: out[0] = 1, out[i] = prod_{j<i} in[j].
  * Replaces accumulate_mul_poly (PLONK/utils/function.cu:256 ->
@@ -219,6 +236,72 @@ int pp_server_cancel(void *server, uint64_t ticket);
 int pp_server_get_stats(void *server, pp_server_stats *stats);
 int pp_server_reset_stats(void *server);
 int pp_server_destroy(void *server);
+
+/* ---------------------------------------------- quotient constraints ---
+ * Element-wise PLONK quotient terms over n points of the extended domain (the
+ * LDE outputs).  Vectors hold n elements; scalars are device pointers to one
+ * element, as the reference passes one-element SyncedMemory buffers.  n = 0
+ * is a no-op.  result may alias none of the inputs except where noted. */
+typedef struct {
+  const void *x;        /* domain points */
+  const void *w[4];     /* w_l, w_r, w_o, w_4 */
+  const void *z;        /* permutation polynomial */
+  const void *z_next;   /* its shift */
+  const void *sigma[4]; /* left, right, out, fourth sigma */
+  const void *mod;      /* vector added by the copy term */
+  const void *l1;       /* first Lagrange polynomial */
+  const void *alpha, *beta, *gamma, *k[3], *one; /* scalars */
+} pp_perm_quotient_args;
+
+/* result[i] = (x b + w_l + g)(x b k1 + w_r + g)(x b k2 + w_o + g)(x b k3 + w_4 + g) z alpha
+ * (b = beta, g = gamma).  Uses x, w, z, alpha, beta, gamma, k.  Replaces
+ * compute_quotient_identity_range_check_i
+ * (PLONK/utils/zkp/cuda/zksnark_compute_permutation_constraint.cu:5-16, :49-78). */
+int pp_quotient_identity(const pp_perm_quotient_args *a, void *d_result, uint64_t n, void *stream);
+/* result[i] += mod[i] - (s_l b + w_l + g)(s_r b + w_r + g)(s_o b + w_o + g)(s_4 b + w_4 + g) z_next alpha
+ * Uses sigma, mod, w, z_next, alpha, beta, gamma.  Replaces
+ * compute_quotient_copy_range_check_i (:18-36, :80-111). */
+int pp_quotient_copy(const pp_perm_quotient_args *a, void *d_result, uint64_t n, void *stream);
+/* result[i] += (z[i] - one) l1[i].  Uses z, l1, one.  Replaces
+ * compute_quotient_term_check_one_i (:38-47, :113-124). */
+int pp_quotient_term_one(const pp_perm_quotient_args *a, void *d_result, uint64_t n, void *stream);
+/* The three above in one pass: result = identity + mod - copy + (z - one) l1,
+ * the value the reference's three launches leave in result.  result is
+ * written only (its old contents are not read). */
+int pp_quotient_permutation(const pp_perm_quotient_args *a, void *d_result, uint64_t n,
+                            void *stream);
+
+/* Gate constraint: the sum of the arithmetic, range, logic, fixed-base and
+ * variable-base group-addition gate terms and the public-input vector.
+ * Replaces compute_gate_constraint_allmerge_cuda / allmerge_kernel
+ * (PLONK/utils/zkp/cuda/zksnark_comute_gate_constraint.cu:5-27, :30-111).
+ * v[] and s[] follow the reference's argument order (PP_GATE_V_*, PP_GATE_S_*).
+ * sbox_alpha is the power x^sbox_alpha of the arithmetic gate; the
+ * reference's mont_t power traps for exponents below 2 (mont_t.cuh:446-449),
+ * here those are refused with PP_E_INVAL, as are exponents >= 2^31. */
+#define PP_GATE_NV 22
+#define PP_GATE_NS 24
+enum {
+  PP_GATE_V_A, PP_GATE_V_B, PP_GATE_V_C, PP_GATE_V_D, PP_GATE_V_A_NEXT, PP_GATE_V_B_NEXT,
+  PP_GATE_V_D_NEXT, PP_GATE_V_Q_M, PP_GATE_V_Q_L, PP_GATE_V_Q_R, PP_GATE_V_Q_O, PP_GATE_V_Q_4,
+  PP_GATE_V_Q_C, PP_GATE_V_Q_HL, PP_GATE_V_Q_HR, PP_GATE_V_Q_H4, PP_GATE_V_Q_ARITH,
+  PP_GATE_V_RANGE, PP_GATE_V_LOGIC, PP_GATE_V_FIXED_GROUP_ADD, PP_GATE_V_VARIABLE_GROUP_ADD,
+  PP_GATE_V_PI
+};
+enum {
+  PP_GATE_S_FOUR, PP_GATE_S_ONE, PP_GATE_S_TWO, PP_GATE_S_THREE, PP_GATE_S_KAPPA_RANGE,
+  PP_GATE_S_KAPPA_SQ_RANGE, PP_GATE_S_KAPPA_CU_RANGE, PP_GATE_S_RANGE_CHALLENGE, PP_GATE_S_P_D,
+  PP_GATE_S_NINE, PP_GATE_S_KAPPA_CU_LOGIC, PP_GATE_S_EIGHTEEN, PP_GATE_S_EIGHTYONE,
+  PP_GATE_S_EIGHTYTHREE, PP_GATE_S_KAPPA_QU_LOGIC, PP_GATE_S_LOGIC_CHALLENGE, PP_GATE_S_P_A,
+  PP_GATE_S_KAPPA_FB, PP_GATE_S_KAPPA_SQ_FB, PP_GATE_S_KAPPA_CU_FB, PP_GATE_S_FB_CHALLENGE,
+  PP_GATE_S_KAPPA_VB, PP_GATE_S_KAPPA_SQ_VB, PP_GATE_S_VB_CHALLENGE
+};
+typedef struct {
+  const void *v[PP_GATE_NV]; /* n-element vectors */
+  const void *s[PP_GATE_NS]; /* one-element scalars */
+  int64_t sbox_alpha;
+} pp_gate_args;
+int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n, void *stream);
 
 /* ----------------------------------------------------------- utilities --- */
 /* n seeded uniformly random canonical elements: element (first_index + i)

@@ -75,6 +75,10 @@ def lib():
                 "or_eval": [v, u, v, v, i], "or_div_xplusc": [v, u, v],
                 "or_naive_gp": [v, u, v], "or_naive_div": [v, u, v, v],
                 "or_first_diff": [v, v, u],
+                "or_quotient_identity": [v, v, v, v, v, v, v, v, u],
+                "or_quotient_copy": [v, v, v, v, v, v, v, v, u],
+                "or_quotient_term_one": [v, v, v, v, u],
+                "or_gate_constraint": [v, v, ctypes.c_int64, v, u],
             }
             for name, args in sigs.items():
                 fn = getattr(L, name)
@@ -284,3 +288,67 @@ def first_diff(a: np.ndarray, b: np.ndarray) -> int:
     if a.shape != b.shape:
         return 0
     return int(lib().or_first_diff(a.ctypes.data, b.ctypes.data, a.shape[0]))
+
+
+# ------------------------------------------------------ quotient constraints
+# argument order of the reference's allmerge_kernel
+# (PLONK/utils/zkp/cuda/zksnark_comute_gate_constraint.cu:6-19)
+GATE_VECTORS = ["a_val", "b_val", "c_val", "d_val", "a_next_eval", "b_next_eval", "d_next_eval",
+                "q_m", "q_l", "q_r", "q_o", "q_4", "q_c", "q_hl", "q_hr", "q_h4", "q_arith",
+                "range", "logic", "fixed_group_add", "variable_group_add", "pi_eval_8n"]
+GATE_SCALARS = ["four", "one", "two", "three", "kappa_range", "kappa_sq_range", "kappa_cu_range",
+                "range_challenge", "P_D", "nine", "kappa_cu_logic", "eighteen", "eightyone",
+                "eightythree", "kappa_qu_logic", "logic_challenge", "P_A", "kappa_fb", "kappa_sq_fb",
+                "kappa_cu_fb", "fb_challenge", "kappa_vb", "kappa_sq_vb", "vb_challenge"]
+
+
+def _vecs(xs):
+    xs = [np.ascontiguousarray(x, dtype=np.uint64) for x in xs]
+    return xs, (ctypes.c_void_p * len(xs))(*[x.ctypes.data for x in xs])
+
+
+def quotient_identity(x, w, z, alpha, beta, gamma, ks) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    z = np.ascontiguousarray(z, dtype=np.uint64)
+    n = x.shape[0]
+    wk, wp = _vecs(w)
+    kk, kp = _vecs([_scalar(k) for k in ks])
+    al, be, ga = _scalar(alpha), _scalar(beta), _scalar(gamma)
+    out = empty(n)
+    lib().or_quotient_identity(x.ctypes.data, ctypes.cast(wp, ctypes.c_void_p), z.ctypes.data,
+                               al.ctypes.data, be.ctypes.data, ga.ctypes.data,
+                               ctypes.cast(kp, ctypes.c_void_p), out.ctypes.data, n)
+    return out
+
+
+def quotient_copy(sigma, mod, w, z_next, alpha, beta, gamma, result) -> np.ndarray:
+    out = np.ascontiguousarray(result, dtype=np.uint64).copy()
+    mod = np.ascontiguousarray(mod, dtype=np.uint64)
+    z_next = np.ascontiguousarray(z_next, dtype=np.uint64)
+    sk, sp = _vecs(sigma)
+    wk, wp = _vecs(w)
+    al, be, ga = _scalar(alpha), _scalar(beta), _scalar(gamma)
+    lib().or_quotient_copy(ctypes.cast(sp, ctypes.c_void_p), mod.ctypes.data,
+                           ctypes.cast(wp, ctypes.c_void_p), z_next.ctypes.data, al.ctypes.data,
+                           be.ctypes.data, ga.ctypes.data, out.ctypes.data, out.shape[0])
+    return out
+
+
+def quotient_term_one(z, l1, one, result) -> np.ndarray:
+    out = np.ascontiguousarray(result, dtype=np.uint64).copy()
+    z = np.ascontiguousarray(z, dtype=np.uint64)
+    l1 = np.ascontiguousarray(l1, dtype=np.uint64)
+    o = _scalar(one)
+    lib().or_quotient_term_one(z.ctypes.data, l1.ctypes.data, o.ctypes.data, out.ctypes.data,
+                               out.shape[0])
+    return out
+
+
+def gate_constraint(vectors: dict, scalars: dict, sbox_alpha: int) -> np.ndarray:
+    vk, vp = _vecs([vectors[k] for k in GATE_VECTORS])
+    sk, sp = _vecs([_scalar(scalars[k]) for k in GATE_SCALARS])
+    n = vk[0].shape[0]
+    out = empty(n)
+    lib().or_gate_constraint(ctypes.cast(vp, ctypes.c_void_p), ctypes.cast(sp, ctypes.c_void_p),
+                             int(sbox_alpha), out.ctypes.data, n)
+    return out

@@ -507,3 +507,146 @@ int64_t or_first_diff(const u64 *a, const u64 *b, u64 n) {
     if (memcmp(a + 4 * i, b + 4 * i, 32) != 0) return (int64_t)i;
   return -1;
 }
+
+/* ------------------------------------------------ quotient constraints ---
+ * Element-wise PLONK quotient terms over the extended domain.  Vectors hold
+ * n elements, scalars one.  Field arithmetic is exact, so the terms may be
+ * grouped and ordered freely; each function follows the formula of the
+ * reference kernel it names. */
+typedef struct {
+  u64 v[4];
+} fe;
+
+static inline fe fe_ld(const u64 *p) {
+  fe r;
+  memcpy(r.v, p, 32);
+  return r;
+}
+static inline fe fm(fe a, fe b) {
+  fe r;
+  mmul(r.v, a.v, b.v);
+  return r;
+}
+static inline fe fa(fe a, fe b) {
+  fe r;
+  madd(r.v, a.v, b.v);
+  return r;
+}
+static inline fe fs(fe a, fe b) {
+  fe r;
+  msub(r.v, a.v, b.v);
+  return r;
+}
+static inline fe fpow_small(fe a, int64_t e) {
+  fe acc = fe_ld(R_ONE);
+  for (int bit = 62; bit >= 0; --bit) {
+    acc = fm(acc, acc);
+    if ((e >> bit) & 1) acc = fm(acc, a);
+  }
+  return acc;
+}
+
+/* zksnark_compute_permutation_constraint.cu:5-16:
+ * (x b + w_l + g)(x b k1 + w_r + g)(x b k2 + w_o + g)(x b k3 + w_4 + g) z alpha */
+void or_quotient_identity(const u64 *x, const u64 *const w[4], const u64 *z, const u64 alpha[4],
+                          const u64 beta[4], const u64 gamma[4], const u64 *const k[3], u64 *result,
+                          u64 n) {
+  const fe al = fe_ld(alpha), be = fe_ld(beta), ga = fe_ld(gamma);
+  for (u64 i = 0; i < n; ++i) {
+    const fe xb = fm(fe_ld(x + 4 * i), be);
+    fe acc = fa(fa(xb, fe_ld(w[0] + 4 * i)), ga);
+    for (int j = 1; j < 4; ++j)
+      acc = fm(acc, fa(fa(fm(xb, fe_ld(k[j - 1])), fe_ld(w[j] + 4 * i)), ga));
+    acc = fm(fm(acc, fe_ld(z + 4 * i)), al);
+    memcpy(result + 4 * i, acc.v, 32);
+  }
+}
+
+/* :18-34: result += mod - (s_l b + w_l + g)(s_r b + w_r + g)(s_o b + w_o + g)(s_4 b + w_4 + g) z' alpha */
+void or_quotient_copy(const u64 *const sigma[4], const u64 *mod, const u64 *const w[4],
+                      const u64 *z_next, const u64 alpha[4], const u64 beta[4], const u64 gamma[4],
+                      u64 *result, u64 n) {
+  const fe al = fe_ld(alpha), be = fe_ld(beta), ga = fe_ld(gamma);
+  for (u64 i = 0; i < n; ++i) {
+    fe acc = fe_ld(R_ONE);
+    for (int j = 0; j < 4; ++j)
+      acc = fm(acc, fa(fa(fm(fe_ld(sigma[j] + 4 * i), be), fe_ld(w[j] + 4 * i)), ga));
+    acc = fm(fm(acc, fe_ld(z_next + 4 * i)), al);
+    const fe r = fs(fa(fe_ld(result + 4 * i), fe_ld(mod + 4 * i)), acc);
+    memcpy(result + 4 * i, r.v, 32);
+  }
+}
+
+/* :36-45: result += (z - one) l1 */
+void or_quotient_term_one(const u64 *z, const u64 *l1, const u64 one[4], u64 *result, u64 n) {
+  const fe o = fe_ld(one);
+  for (u64 i = 0; i < n; ++i) {
+    const fe r = fa(fe_ld(result + 4 * i), fm(fs(fe_ld(z + 4 * i), o), fe_ld(l1 + 4 * i)));
+    memcpy(result + 4 * i, r.v, 32);
+  }
+}
+
+/* zksnark_comute_gate_constraint.cu:6-30 (allmerge_kernel), the sum of six
+ * gate terms.  v[] holds the 22 vectors and s[] the 24 scalars in the order of
+ * the kernel's arguments (PP_GATE_V_* / PP_GATE_S_* in include/pp_ops.h).
+ * The reference writes d - (d - d_next) for d_next and forms its range/logic
+ * "delta" as x (x three)((x one)(x two)) = x^4 * three * one * two. */
+void or_gate_constraint(const u64 *const v[22], const u64 *const s[24], int64_t sbox_alpha,
+                        u64 *out, u64 n) {
+  fe S[24];
+  for (int j = 0; j < 24; ++j) S[j] = fe_ld(s[j]);
+  const fe four = S[0], one = S[1], two = S[2], three = S[3], kr = S[4], ksr = S[5], kcr = S[6],
+           rch = S[7], pd = S[8], nine = S[9], kcl = S[10], e18 = S[11], e81 = S[12], e83 = S[13],
+           kql = S[14], lch = S[15], pa = S[16], kfb = S[17], ksfb = S[18], kcfb = S[19],
+           fbch = S[20], kvb = S[21], ksvb = S[22], vbch = S[23];
+  const fe k312 = fm(fm(three, one), two);
+  for (u64 i = 0; i < n; ++i) {
+    fe V[22];
+    for (int j = 0; j < 22; ++j) V[j] = fe_ld(v[j] + 4 * i);
+    const fe a = V[0], b = V[1], c = V[2], d = V[3], an = V[4], bn = V[5], dn = V[6], qm = V[7],
+             ql = V[8], qr = V[9], qo = V[10], q4 = V[11], qc = V[12], qhl = V[13], qhr = V[14],
+             qh4 = V[15], qar = V[16], rng = V[17], lgc = V[18], fga = V[19], vga = V[20],
+             pi = V[21];
+#define DELTA(x) fm(fm(fm((x), (x)), fm((x), (x))), k312)
+    const fe a4 = fm(a, four), b4 = fm(b, four), c4 = fm(c, four), d4 = fm(d, four);
+    /* range */
+    const fe rg = fm(fm(fa(fa(fa(fm(DELTA(fs(a4, dn)), kcr), fm(DELTA(fs(a, b4)), ksr)),
+                              DELTA(fs(c, d4))),
+                           fm(DELTA(fs(b, c4)), kr)),
+                        rch),
+                     rng);
+    /* logic */
+    const fe da = fs(a4, an), db = fs(b4, bn), w = fa(da, db), e = fs(dn, d4);
+    const fe da2 = fm(da, da);
+    const fe inner = fs(fm(w, e81), fa(fm(c, fm(fs(c4, fm(w, e18)), e81)), fm(fa(da2, da2), e18)));
+    const fe A = fs(fm(fa(e, w), three), fm(fm(c, fm(inner, e83)), two));
+    const fe B = fm(qc, fs(fm(e, nine), fm(w, three)));
+    const fe lg = fm(fm(fa(fa(fa(fa(fm(fa(A, B), kql), fm(fs(c, fm(da, db)), kcl)), DELTA(e)),
+                              DELTA(da)),
+                           DELTA(db)),
+                        lch),
+                     lgc);
+#undef DELTA
+    /* arithmetic */
+    fe ar = fa(fm(fpow_small(d, sbox_alpha), qh4), fm(fpow_small(b, sbox_alpha), qhr));
+    ar = fa(ar, fm(fpow_small(a, sbox_alpha), qhl));
+    ar = fa(fa(fa(ar, fm(d, q4)), fm(c, qo)), fm(b, qr));
+    ar = fa(fa(fa(ar, fm(fm(a, b), qm)), fm(a, ql)), qc);
+    ar = fm(ar, qar);
+    /* fixed-base group addition */
+    const fe abc = fm(fm(a, b), c);
+    const fe qr2 = fm(fm(qr, fm(dn, dn)), fm(one, one));
+    const fe f1 = fm(fs(c, fm(qc, dn)), kfb);
+    const fe f2 = fm(fs(fs(bn, fm(fm(abc, bn), pd)), fs(fm(b, qr2), fm(a, fm(fm(ql, dn), pa)))), kcfb);
+    const fe f3 = fm(fm(fm(dn, dn), dn), fm(one, one));
+    const fe f4 = fm(fs(fa(an, fm(fm(abc, an), pd)), fa(fm(b, fm(ql, dn)), fm(a, qr2))), ksfb);
+    const fe fb = fm(fm(fa(fa(fa(f1, f2), f3), f4), fbch), fga);
+    /* variable-base group addition */
+    const fe bc = fm(b, c);
+    const fe v1 = fm(fs(fs(fm(b, d), fm(fm(a, c), pa)), fs(bn, fm(bc, fm(dn, fm(bn, pd))))), ksvb);
+    const fe v2 = fa(fs(dn, fm(a, d)), fm(fs(fa(dn, bc), fa(an, fm(bc, fm(dn, fm(an, pd))))), kvb));
+    const fe vb = fm(fm(fa(v1, v2), vbch), vga);
+    const fe r = fa(fa(fa(fa(fa(fb, lg), rg), ar), pi), vb);
+    memcpy(out + 4 * i, r.v, 32);
+  }
+}

@@ -53,6 +53,20 @@ void or_div_xplusc(uint64_t *inout, uint64_t n, const uint64_t c[4]);
 void or_naive_gp(const uint64_t *in, uint64_t n, uint64_t *out);
 int or_naive_div(const uint64_t *in, uint64_t n, const uint64_t c[4], uint64_t *quotient);
 
+/* PLONK quotient constraints (element-wise over the extended domain):
+ * zksnark_compute_permutation_constraint.cu:5-47 and
+ * zksnark_comute_gate_constraint.cu:6-30.  Scalars are one element. */
+void or_quotient_identity(const uint64_t *x, const uint64_t *const w[4], const uint64_t *z,
+                          const uint64_t alpha[4], const uint64_t beta[4], const uint64_t gamma[4],
+                          const uint64_t *const k[3], uint64_t *result, uint64_t n);
+void or_quotient_copy(const uint64_t *const sigma[4], const uint64_t *mod, const uint64_t *const w[4],
+                      const uint64_t *z_next, const uint64_t alpha[4], const uint64_t beta[4],
+                      const uint64_t gamma[4], uint64_t *result, uint64_t n);
+void or_quotient_term_one(const uint64_t *z, const uint64_t *l1, const uint64_t one[4],
+                          uint64_t *result, uint64_t n);
+void or_gate_constraint(const uint64_t *const v[22], const uint64_t *const s[24], int64_t sbox_alpha,
+                        uint64_t *out, uint64_t n);
+
 /* bit-exact byte comparison helper: index of first differing element or -1 */
 int64_t or_first_diff(const uint64_t *a, const uint64_t *b, uint64_t n);
 

@@ -164,37 +164,71 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
     out_base = (kb << a.lgT) + (rest << lgR1);
   }
 
-  // ---- load the tile (coalesced) into shared memory
-  for (uint32_t e = tid; active && e < E; e += nthr) {
-    uint32_t n, col;
-    uint64_t g;
-    if (!a.last) {
-      n = e >> a.lgT;
-      col = e & (T - 1);
-      g = base + ((uint64_t)n << a.lgS) + col;
-    } else if (a.P == 1) {
-      n = e;
-      col = 0;
-      g = n;
-    } else {
-      n = e & (R - 1);
-      col = e >> a.lgR;
-      g = in_base + ((uint64_t)col << lgS1) + n;
-    }
-    fr v;
-    if (a.first) {
-      if (a.in_kind == NTT_IN_SPREAD) {
-        v = (g & ((1ull << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (g >> a.spread)) : fr_zero();
-      } else if (g < a.n_valid) {
-        v = ldcs_fr(a.in + g);
-        if (a.in_kind == NTT_IN_DIAG) v = fr_mul(v, ldcs_fr(a.diag + g));
+  // ---- load the tile (coalesced) into shared memory.  A host-memory input
+  // without a multiply on the way in moves 16-byte halves, so one warp
+  // instruction reads whole 128-byte lines.
+  if (a.unit_in && !(a.first && a.in_kind == NTT_IN_DIAG)) {
+    const uint4 zero4 = make_uint4(0, 0, 0, 0);
+    for (uint32_t u = tid; active && u < 2 * E; u += nthr) {
+      const uint32_t e = u >> 1, h = u & 1;
+      uint32_t n, col;
+      uint64_t g;
+      if (!a.last) {
+        n = e >> a.lgT;
+        col = e & (T - 1);
+        g = base + ((uint64_t)n << a.lgS) + col;
+      } else if (a.P == 1) {
+        n = e;
+        col = 0;
+        g = n;
       } else {
-        v = fr_zero();
+        n = e & (R - 1);
+        col = e >> a.lgR;
+        g = in_base + ((uint64_t)col << lgS1) + n;
       }
-    } else {
-      v = ldcs_fr(a.in + g);
+      uint4 v = zero4;
+      if (!a.first) {
+        v = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
+      } else if (a.in_kind == NTT_IN_SPREAD) {
+        if ((g & ((1ull << a.spread) - 1)) == 0)
+          v = __ldcs(reinterpret_cast<const uint4 *>(a.in + (g >> a.spread)) + h);
+      } else if (g < a.n_valid) {
+        v = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
+      }
+      tile.s[swz((((n << a.lgT) + col) << 1) + h)] = v;
     }
-    tile.put(n, col, v);
+  } else {
+    for (uint32_t e = tid; active && e < E; e += nthr) {
+      uint32_t n, col;
+      uint64_t g;
+      if (!a.last) {
+        n = e >> a.lgT;
+        col = e & (T - 1);
+        g = base + ((uint64_t)n << a.lgS) + col;
+      } else if (a.P == 1) {
+        n = e;
+        col = 0;
+        g = n;
+      } else {
+        n = e & (R - 1);
+        col = e >> a.lgR;
+        g = in_base + ((uint64_t)col << lgS1) + n;
+      }
+      fr v;
+      if (a.first) {
+        if (a.in_kind == NTT_IN_SPREAD) {
+          v = (g & ((1ull << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (g >> a.spread)) : fr_zero();
+        } else if (g < a.n_valid) {
+          v = ldcs_fr(a.in + g);
+          if (a.in_kind == NTT_IN_DIAG) v = fr_mul(v, ldcs_fr(a.diag + g));
+        } else {
+          v = fr_zero();
+        }
+      } else {
+        v = ldcs_fr(a.in + g);
+      }
+      tile.put(n, col, v);
+    }
   }
   __syncthreads();
 
@@ -262,7 +296,27 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
     }
   }
 
-  // ---- store (coalesced), with the layer twiddle or the final scale
+  // ---- store (coalesced), with the layer twiddle or the final scale.  A
+  // host-memory output without a scale moves 16-byte halves, so one warp
+  // instruction writes whole 128-byte lines (partial lines cost C2C bandwidth).
+  if (a.last && a.unit_out && !a.has_post_scale) {
+    for (uint32_t u = tid; active && u < 2 * E; u += nthr) {
+      const uint32_t e = u >> 1, h = u & 1;
+      uint32_t o, col;
+      if (a.P == 1) {
+        o = e;
+        col = 0;
+      } else {
+        o = e >> a.lgT;
+        col = e & (T - 1);
+      }
+      const uint4 v = tile.s[swz((((digit_reverse(o, a.lgR) << a.lgT) + col) << 1) + h)];
+      const uint64_t g =
+          a.P == 1 ? (uint64_t)o : out_base + col + ((uint64_t)o << (a.lgN - a.lgR));
+      reinterpret_cast<uint4 *>(a.out + g)[h] = v;
+    }
+    return;
+  }
   for (uint32_t e = tid; active && e < E; e += nthr) {
     uint32_t o, col;
     if (a.P == 1) {
@@ -653,6 +707,8 @@ int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool invers
     a.lgS = lg_m - acc;
     a.first = j == 0;
     a.last = j + 1 == plan->P;
+    a.unit_in = a.first && in.in_host;
+    a.unit_out = a.last && in.out_host;
     a.in = j == 0 ? d_in : work;
     a.out = a.last ? d_out : work;
     a.tw_inner = plan->tw_inner[j];

@@ -20,6 +20,7 @@ struct PassArgs {
   uint64_t n_valid;
   uint32_t lgR, lgT, lgS, lgN;
   uint32_t first, last, has_post_scale, in_kind, spread;
+  uint32_t unit_in, unit_out;  // move 16-byte halves (host-memory input / output)
   uint32_t P;
   uint32_t lgRp[4];
 };
@@ -41,6 +42,11 @@ struct NttInputDesc {
   const fr *diag = nullptr;
   uint64_t n_valid = 0;  // 0 = all 2^lg_m
   uint32_t spread = 0;
+  // the input / output is page-locked host memory: the first pass reads and
+  // the last pass writes in 16-byte halves, so every warp access covers whole
+  // 128-byte lines of the NVLink-C2C traffic
+  bool in_host = false;
+  bool out_host = false;
 };
 
 // Runs the transform of 2^lg_m points: d_in -> d_out (may alias), on stream.

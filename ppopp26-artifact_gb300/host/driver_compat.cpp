@@ -12,6 +12,12 @@
 //       byte for byte and Intt::forward against the input (ntt.cu:1276-1351)
 //   pp_compat_driver lde <lg_N> <lambda> <in.bin> <out.bin> [naive]
 //       our_lde (or naive_lde) -> out.bin
+//   pp_compat_driver quotient <n> <dir>
+//       compute_quotient_identity_range_check_i, then ..._copy_... and
+//       ..._term_check_one_i on one result buffer, as the prover calls them;
+//       inputs <dir>/<argument name>.bin -> <dir>/quotient_out.bin
+//   pp_compat_driver gate <n> <sbox_alpha> <dir>
+//       compute_gate_constraint_allmerge_cuda -> <dir>/gate_out.bin
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -19,6 +25,7 @@
 #include <vector>
 
 #include "function.h"
+#include "zksnark.h"
 
 static std::vector<unsigned char> read_file(const std::string &path, size_t bytes) {
   std::vector<unsigned char> v(bytes);
@@ -110,10 +117,51 @@ static int lde(int lg, int lambda, const std::string &in, const std::string &out
   return 0;
 }
 
+static int quotient(size_t n, const std::string &dir) {
+  auto V = [&](const char *name) { return load(dir + "/" + name + ".bin", n); };
+  auto S = [&](const char *name) { return load(dir + "/" + name + ".bin", 1); };
+  SyncedMemory result = V("result");
+  cuda::compute_quotient_identity_range_check_i(V("x"), V("w_l"), V("w_r"), V("w_o"), V("w_4"),
+                                                V("z"), S("alpha"), S("beta"), S("gamma"), S("k1"),
+                                                S("k2"), S("k3"), result);
+  cuda::compute_quotient_copy_range_check_i(V("left_sigma"), V("right_sigma"), V("out_sigma"),
+                                            V("fourth_sigma"), V("mod"), V("w_l"), V("w_r"),
+                                            V("w_o"), V("w_4"), V("z_next"), S("alpha"), S("beta"),
+                                            S("gamma"), result);
+  cuda::compute_quotient_term_check_one_i(V("z"), V("l1"), S("one"), result);
+  cudaDeviceSynchronize();
+  write_file(dir + "/quotient_out.bin", result.mutable_cpu_data(), n * 32);
+  std::printf("quotient ok\n");
+  return 0;
+}
+
+static int gate(size_t n, long long alpha, const std::string &dir) {
+  auto V = [&](const char *name) { return load(dir + "/" + name + ".bin", n); };
+  auto S = [&](const char *name) { return load(dir + "/" + name + ".bin", 1); };
+  SyncedMemory out = cuda::compute_gate_constraint_allmerge_cuda(
+      V("a_val"), V("b_val"), V("c_val"), V("d_val"), V("a_next_eval"), V("b_next_eval"),
+      V("d_next_eval"), V("q_m"), V("q_l"), V("q_r"), V("q_o"), V("q_4"), V("q_c"), V("q_hl"),
+      V("q_hr"), V("q_h4"), V("q_arith"), V("range"), V("logic"), V("fixed_group_add"),
+      V("variable_group_add"), V("pi_eval_8n"), S("four"), S("one"), S("two"), S("three"),
+      S("kappa_range"), S("kappa_sq_range"), S("kappa_cu_range"), S("range_challenge"), S("P_D"),
+      S("nine"), S("kappa_cu_logic"), S("eighteen"), S("eightyone"), S("eightythree"),
+      S("kappa_qu_logic"), S("logic_challenge"), S("P_A"), S("kappa_fb"), S("kappa_sq_fb"),
+      S("kappa_cu_fb"), S("fb_challenge"), S("kappa_vb"), S("kappa_sq_vb"), S("vb_challenge"),
+      alpha);
+  cudaDeviceSynchronize();
+  write_file(dir + "/gate_out.bin", out.mutable_cpu_data(), n * 32);
+  std::printf("gate ok\n");
+  return 0;
+}
+
 int main(int argc, char **argv) {
   try {
     if (argc >= 5 && std::string(argv[1]) == "miss_ops") return miss_ops(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 5 && std::string(argv[1]) == "ntt") return ntt_check(std::atoi(argv[2]), argv[3], argv[4]);
+    if (argc >= 4 && std::string(argv[1]) == "quotient")
+      return quotient(std::strtoull(argv[2], nullptr, 10), argv[3]);
+    if (argc >= 5 && std::string(argv[1]) == "gate")
+      return gate(std::strtoull(argv[2], nullptr, 10), std::atoll(argv[3]), argv[4]);
     if (argc >= 6 && std::string(argv[1]) == "lde")
       return lde(std::atoi(argv[2]), std::atoi(argv[3]), argv[4], argv[5],
                  argc >= 7 && std::string(argv[6]) == "naive");
@@ -121,6 +169,6 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
     return 3;
   }
-  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde ...\n", argv[0]);
+  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate ...\n", argv[0]);
   return 1;
 }

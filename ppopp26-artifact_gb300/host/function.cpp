@@ -86,6 +86,41 @@ int lde_op(void *din, void *dout, void *ctx) {
   const LdeCtx *c = static_cast<const LdeCtx *>(ctx);
   return pp_lde(din, dout, c->lg, c->lambda, c->mode, nullptr);
 }
+int ntt_host_op(void *hin, void *hout, void *ctx) {
+  const NttCtx *c = static_cast<const NttCtx *>(ctx);
+  return pp_ntt_host(hin, hout, c->lg, c->inverse, nullptr);
+}
+int lde_host_op(void *hin, void *hout, void *ctx) {
+  const LdeCtx *c = static_cast<const LdeCtx *>(ctx);
+  return pp_lde_host(hin, hout, c->lg, c->lambda, c->mode, nullptr);
+}
+
+bool page_locked(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+}
+
+// page-locked host buffer in, page-locked host buffer out, no staging copy:
+// the transform's first pass reads host memory and its last pass writes it
+float host_direct(void *host_in, void *host_out, const char *what, int (*op)(void *, void *, void *),
+                  void *ctx) {
+  cudaEvent_t e0, e1;
+  pp::check_cuda(cudaEventCreate(&e0), "cudaEventCreate");
+  pp::check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+  cudaDeviceSynchronize();
+  cudaEventRecord(e0, 0);
+  pp::check(op(host_in, host_out, ctx), what);
+  cudaEventRecord(e1, 0);
+  pp::check_cuda(cudaEventSynchronize(e1), what);
+  const float ms = elapsed(e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
 
 }  // namespace
 
@@ -159,9 +194,11 @@ void our_ntt(SyncedMemory input, int lg_N, int, int, int, int, int, Ntt ntt, con
   const size_t n = fr_count(input, "our_ntt");
   if (n != (size_t{1} << lg_N)) throw pp::Error(PP_E_INVAL, "our_ntt: buffer length is not 2^lg_N");
   if (lg_N > ntt.max_lg()) throw pp::Error(PP_E_UNSUPPORTED, "our_ntt: larger than the Ntt domain");
+  // SyncedMemory's host side is page-locked: transform it where it lies
   void *h = input.mutable_cpu_data();
   NttCtx ctx{(uint32_t)lg_N, 0};
-  const float ms = host_roundtrip(h, n * kFr, h, n * kFr, "our_ntt", ntt_op, &ctx);
+  const float ms = page_locked(h) ? host_direct(h, h, "our_ntt", ntt_host_op, &ctx)
+                                  : host_roundtrip(h, n * kFr, h, n * kFr, "our_ntt", ntt_op, &ctx);
   std::printf("our-ntt execution time: %g ms\n", ms);
 }
 
@@ -176,24 +213,26 @@ void standard4_ntt(SyncedMemory input, int lg_N, int, int, int, int, Ntt ntt) {
 }
 
 static float lde_driver(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, uint32_t mode, Ntt &ntt,
-                        const char *what) {
+                        const char *what, bool direct_ok) {
   if (lg_N < 0 || lambda < 0 || lg_N + lambda > ntt.max_lg())
     throw pp::Error(PP_E_UNSUPPORTED, std::string(what) + ": 2^(lg_N+lambda) exceeds the Ntt domain");
   const size_t n = size_t{1} << lg_N, m = n << lambda;
   g_last_lde = SyncedMemory(m * kFr);
   void *hout = g_last_lde.mutable_cpu_data();
   LdeCtx ctx{(uint32_t)lg_N, (uint32_t)lambda, mode};
+  // a page-locked caller buffer is read in place; a pageable one is staged
+  if (direct_ok && page_locked(input)) return host_direct(input, hout, what, lde_host_op, &ctx);
   return host_roundtrip(input, n * kFr, hout, m * kFr, what, lde_op, &ctx);
 }
 
 float our_lde(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, int, int, int, Ntt &ntt) {
-  const float ms = lde_driver(input, lg_N, lambda, PP_LDE_COEFFS, ntt, "our_lde");
+  const float ms = lde_driver(input, lg_N, lambda, PP_LDE_COEFFS, ntt, "our_lde", true);
   std::printf("our-lde execution time: %g ms\n", ms);
   return ms;
 }
 
 float naive_lde(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, int, int, int, Ntt &ntt) {
-  const float ms = lde_driver(input, lg_N, lambda, PP_LDE_SPREAD, ntt, "naive_lde");
+  const float ms = lde_driver(input, lg_N, lambda, PP_LDE_SPREAD, ntt, "naive_lde", false);
   std::printf("naive-lde execution time: %g ms\n", ms);
   return ms;
 }

@@ -14,12 +14,16 @@
 //   lde.cu:1367                  naive_lde(input, lg_N, lambda, lg_k, ...)
 //
 // The reference's segmented drivers (our_ntt, our_lde, standard4_ntt,
-// naive_lde) stream host-resident data through the GPU in chunks; on GB300
-// the whole problem fits in HBM, so here they copy the host buffer to the
-// device once, run the in-HBM transform and copy the result back.  Their
-// segmentation and CPU-thread arguments are accepted for source
-// compatibility and do not change the result (which the reference's own
-// --check-* modes require to equal Ntt::forward bit for bit).
+// naive_lde) stream host-resident data through the GPU in chunks and permute
+// on the CPU.  On GB300 the whole problem fits in HBM and the GPU reaches
+// page-locked host memory directly: our_ntt and our_lde run pp_ntt_host /
+// pp_lde_host, whose first pass reads the host input and whose last pass
+// writes the host output, with only the middle passes in HBM.  A pageable
+// caller buffer (our_lde's input), standard4_ntt and naive_lde take the
+// staged form instead: one copy in, the in-HBM transform, one copy out.  The
+// segmentation and CPU-thread arguments are accepted for source compatibility
+// and do not change the result (which the reference's own --check-* modes
+// require to equal Ntt::forward bit for bit).
 #pragma once
 #include <cstdint>
 

@@ -41,6 +41,8 @@ def lib():
             proto = {
                 "pp_ntt": [v, v, u32, i, v],
                 "pp_lde": [v, v, u32, u32, u32, v],
+                "pp_ntt_host": [v, v, u32, i, v],
+                "pp_lde_host": [v, v, u32, u32, u32, v],
                 "pp_gp_prefix": [v, u64, v],
                 "pp_gp_perm": [v, v, v, v, u32, v],
                 "pp_eval": [v, u64, v, v, v],
@@ -129,6 +131,130 @@ def lde(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):
     if out is None:
         out = empty(x.shape[0] << lam, x.device)
     check(lib().pp_lde(_ptr(x), _ptr(out), lg, lam, mode, _stream(stream)))
+    return out
+
+
+def _hptr(t):
+    assert (not t.is_cuda) and t.is_contiguous() and t.dtype == _torch().int64, \
+        "need a contiguous int64 host tensor"
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def empty_pinned(n: int):
+    return _torch().empty((n, 4), dtype=_torch().int64, pin_memory=True)
+
+
+def ntt_host(x, inverse: bool = False, out=None, stream=None):
+    """Transform of a page-locked host tensor into a page-locked host tensor
+    (pp_ntt_host).  Asynchronous: synchronise the stream before reading out."""
+    lg = _lg(x.shape[0])
+    if out is None:
+        out = empty_pinned(x.shape[0])
+    check(lib().pp_ntt_host(_hptr(x), _hptr(out), lg, int(inverse), _stream(stream)))
+    return out
+
+
+def lde_host(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):
+    """pp_lde_host: page-locked host input and output."""
+    lg = _lg(x.shape[0])
+    if out is None:
+        out = empty_pinned(x.shape[0] << lam)
+    check(lib().pp_lde_host(_hptr(x), _hptr(out), lg, lam, mode, _stream(stream)))
+    return out
+
+
+# ------------------------------------------------------ quotient constraints
+class PermQuotientArgs(ctypes.Structure):
+    """pp_perm_quotient_args (include/pp_ops.h)."""
+    _fields_ = [("x", ctypes.c_void_p), ("w", ctypes.c_void_p * 4), ("z", ctypes.c_void_p),
+                ("z_next", ctypes.c_void_p), ("sigma", ctypes.c_void_p * 4), ("mod", ctypes.c_void_p),
+                ("l1", ctypes.c_void_p), ("alpha", ctypes.c_void_p), ("beta", ctypes.c_void_p),
+                ("gamma", ctypes.c_void_p), ("k", ctypes.c_void_p * 3), ("one", ctypes.c_void_p)]
+
+
+# argument order of the reference's compute_gate_constraint_allmerge_cuda
+GATE_VECTORS = ["a_val", "b_val", "c_val", "d_val", "a_next_eval", "b_next_eval", "d_next_eval",
+                "q_m", "q_l", "q_r", "q_o", "q_4", "q_c", "q_hl", "q_hr", "q_h4", "q_arith",
+                "range", "logic", "fixed_group_add", "variable_group_add", "pi_eval_8n"]
+GATE_SCALARS = ["four", "one", "two", "three", "kappa_range", "kappa_sq_range", "kappa_cu_range",
+                "range_challenge", "P_D", "nine", "kappa_cu_logic", "eighteen", "eightyone",
+                "eightythree", "kappa_qu_logic", "logic_challenge", "P_A", "kappa_fb", "kappa_sq_fb",
+                "kappa_cu_fb", "fb_challenge", "kappa_vb", "kappa_sq_vb", "vb_challenge"]
+
+
+class GateArgs(ctypes.Structure):
+    """pp_gate_args (include/pp_ops.h)."""
+    _fields_ = [("v", ctypes.c_void_p * len(GATE_VECTORS)), ("s", ctypes.c_void_p * len(GATE_SCALARS)),
+                ("sbox_alpha", ctypes.c_int64)]
+
+
+def _opt(t):
+    return None if t is None else _ptr(t).value
+
+
+def _perm_args(x=None, w=None, z=None, z_next=None, sigma=None, mod=None, l1=None, alpha=None,
+               beta=None, gamma=None, k=None, one=None):
+    a = PermQuotientArgs()
+    a.x, a.z, a.z_next, a.mod, a.l1 = _opt(x), _opt(z), _opt(z_next), _opt(mod), _opt(l1)
+    a.alpha, a.beta, a.gamma, a.one = _opt(alpha), _opt(beta), _opt(gamma), _opt(one)
+    for j in range(4):
+        a.w[j] = _opt(w[j]) if w is not None else None
+        a.sigma[j] = _opt(sigma[j]) if sigma is not None else None
+    for j in range(3):
+        a.k[j] = _opt(k[j]) if k is not None else None
+    return a
+
+
+def _perm_call(name, args, result, stream):
+    fn = getattr(lib(), name)
+    fn.argtypes = [ctypes.POINTER(PermQuotientArgs), ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    check(fn(ctypes.byref(args), _ptr(result), result.shape[0], _stream(stream)))
+    return result
+
+
+def quotient_identity(x, w, z, alpha, beta, gamma, k, out=None, stream=None):
+    """pp_quotient_identity: (x b + w_l + g)(x b k1 + w_r + g)(x b k2 + w_o + g)(x b k3 + w_4 + g) z alpha."""
+    out = empty(x.shape[0], x.device) if out is None else out
+    return _perm_call("pp_quotient_identity",
+                      _perm_args(x=x, w=w, z=z, alpha=alpha, beta=beta, gamma=gamma, k=k), out, stream)
+
+
+def quotient_copy_(result, sigma, mod, w, z_next, alpha, beta, gamma, stream=None):
+    """pp_quotient_copy, in place on result."""
+    return _perm_call("pp_quotient_copy", _perm_args(sigma=sigma, mod=mod, w=w, z_next=z_next,
+                                                     alpha=alpha, beta=beta, gamma=gamma), result, stream)
+
+
+def quotient_term_one_(result, z, l1, one, stream=None):
+    """pp_quotient_term_one, in place on result."""
+    return _perm_call("pp_quotient_term_one", _perm_args(z=z, l1=l1, one=one), result, stream)
+
+
+def quotient_permutation(x, w, z, z_next, sigma, mod, l1, alpha, beta, gamma, k, one, out=None,
+                         stream=None):
+    """pp_quotient_permutation: the three permutation terms in one pass."""
+    out = empty(x.shape[0], x.device) if out is None else out
+    return _perm_call("pp_quotient_permutation",
+                      _perm_args(x=x, w=w, z=z, z_next=z_next, sigma=sigma, mod=mod, l1=l1, alpha=alpha,
+                                 beta=beta, gamma=gamma, k=k, one=one), out, stream)
+
+
+def gate_constraint(vectors: dict, scalars: dict, sbox_alpha: int, out=None, stream=None):
+    """pp_gate_constraint; vectors / scalars keyed by the reference's argument names."""
+    a = GateArgs()
+    for j, name in enumerate(GATE_VECTORS):
+        a.v[j] = _ptr(vectors[name]).value
+    for j, name in enumerate(GATE_SCALARS):
+        a.s[j] = _ptr(scalars[name]).value
+    a.sbox_alpha = int(sbox_alpha)
+    first = vectors[GATE_VECTORS[0]]
+    out = empty(first.shape[0], first.device) if out is None else out
+    L = lib()
+    L.pp_gate_constraint.argtypes = [ctypes.POINTER(GateArgs), ctypes.c_void_p, ctypes.c_uint64,
+                                     ctypes.c_void_p]
+    L.pp_gate_constraint.restype = ctypes.c_int
+    check(L.pp_gate_constraint(ctypes.byref(a), _ptr(out), out.shape[0], _stream(stream)))
     return out
 
 

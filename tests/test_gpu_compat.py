@@ -63,3 +63,38 @@ def test_lde_driver(pp, O, cuda, tmp_path, lg, lam):
     assert O.first_diff(load(tmp_path / "out.bin", n << lam), O.lde_coeffs(x, lam)) == -1
     run("lde", lg, lam, tmp_path / "in.bin", tmp_path / "out2.bin", "naive")
     assert O.first_diff(load(tmp_path / "out2.bin", n << lam), O.lde_spread(x, lam)) == -1
+
+
+GOLD = os.path.join(ROOT, "tests", "golden", "constraints.npz")
+
+
+@pytest.mark.parametrize("n", [7, 64])
+def test_quotient_driver_matches_golden(pp, O, cuda, tmp_path, n):
+    """The three permutation-term entry points, called in sequence on one
+    result buffer as the prover does, through the C++ layer."""
+    g = np.load(GOLD)
+    t = "perm_n%d/" % n
+    for k in g.files:
+        if k.startswith(t):
+            np.ascontiguousarray(g[k]).tofile(tmp_path / (k[len(t):] + ".bin"))
+    run("quotient", n, tmp_path)
+    # identity writes result, copy and term-one add to it
+    want = g[t + "identity"]
+    w = [g[t + k] for k in ("w_l", "w_r", "w_o", "w_4")]
+    sig = [g[t + k] for k in ("left_sigma", "right_sigma", "out_sigma", "fourth_sigma")]
+    want = O.quotient_copy(sig, g[t + "mod"], w, g[t + "z_next"], g[t + "alpha"][0], g[t + "beta"][0],
+                           g[t + "gamma"][0], want)
+    want = O.quotient_term_one(g[t + "z"], g[t + "l1"], g[t + "one"][0], want)
+    assert np.array_equal(load(tmp_path / "quotient_out.bin", n), want)
+
+
+@pytest.mark.parametrize("case", ["gate_rand_a5_n64", "gate_small_a5_n33", "gate_rand_a2_n16"])
+def test_gate_driver_matches_golden(pp, cuda, tmp_path, case):
+    g = np.load(GOLD)
+    t = case + "/"
+    for k in g.files:
+        if k.startswith(t) and not k.endswith("SBOX_ALPHA"):
+            np.ascontiguousarray(g[k]).tofile(tmp_path / (k[len(t):] + ".bin"))
+    n = g[t + "out"].shape[0]
+    run("gate", n, int(g[t + "SBOX_ALPHA"][0]), tmp_path)
+    assert np.array_equal(load(tmp_path / "gate_out.bin", n), g[t + "out"])
