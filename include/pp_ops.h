@@ -303,6 +303,24 @@ typedef struct {
 } pp_gate_args;
 int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n, void *stream);
 
+/* -------------------------------------------------------- data formats ---
+ * The reference's element files are raw 32-byte little-endian Montgomery
+ * elements (read_file miss_ops.cu:8-24, read_file_exact lde.cu:222-231);
+ * host/io.h reads and writes them.  These convert on the device:
+ *   pp_to_mont: a -> a R mod r (any 256-bit a; canonical output).  Replaces
+ *     to_mont (PLONK/utils/function.cu:5-12 -> mont_arithmetic.cu:57-63,
+ *     :222-229, :372-389; mont_t::to, mont_t.cuh:473).
+ *   pp_to_base: a -> a R^-1 mod r, back to plain integers.  Replaces to_base
+ *     (function.cu:14-21 -> mont_arithmetic.cu:65-71, :231-238, :391-411;
+ *     mont_t::from, mont_t.cuh:503).
+ * d_in == d_out is allowed.  n = 0 is a no-op. */
+int pp_to_mont(const void *d_in, void *d_out, uint64_t n, void *stream);
+int pp_to_base(const void *d_in, void *d_out, uint64_t n, void *stream);
+/* *d_count = number of elements of d_in that are >= r (not canonical), e.g.
+ * to validate a raw file before it enters the operators.  d_count is a device
+ * pointer; the count is written asynchronously on the stream. */
+int pp_count_noncanonical(const void *d_in, uint64_t n, uint64_t *d_count, void *stream);
+
 /* ----------------------------------------------------------- utilities --- */
 /* n seeded uniformly random canonical elements: element (first_index + i)
  * limb j is the SplitMix64 output at counter ((first_index+i) << 8 | t << 2 | j)

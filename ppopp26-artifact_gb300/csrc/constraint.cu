@@ -77,8 +77,18 @@ __global__ void __launch_bounds__(kThreads) k_perm_quotient(const PermArgs a, fr
 struct GateArgs {
   const fr *v[PP_GATE_NV];
   const fr *s[PP_GATE_NS];
-  uint64_t sbox_alpha;
+  uint32_t sbox_alpha;  // 2 <= sbox_alpha < 2^31
 };
+
+// x^e for 2 <= e < 2^31, square and multiply from the top set bit
+__device__ __forceinline__ fr pow_small(const fr &x, uint32_t e) {
+  fr r = x;
+  for (int b = 30 - __clz(e); b >= 0; --b) {
+    r = fr_mul(r, r);
+    if ((e >> b) & 1) r = fr_mul(r, x);
+  }
+  return r;
+}
 
 // x^4 * three * one * two: the reference's x (x three)((x one)(x two))
 __device__ __forceinline__ fr delta4(const fr &x, const fr &k312) {
@@ -86,22 +96,30 @@ __device__ __forceinline__ fr delta4(const fr &x, const fr &k312) {
   return fr_mul(fr_mul(x2, x2), k312);
 }
 
-__global__ void __launch_bounds__(kThreads) k_gate_constraint(const GateArgs a, fr *out,
-                                                              uint64_t n) {
-  __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
+// The gate runs as three launches so that each keeps its live values in
+// fewer registers (more resident warps): the range and logic terms are
+// written first, then the arithmetic and public-input terms and the fixed-
+// and variable-base group additions are added.
+__device__ __forceinline__ void stage_scalars(const GateArgs &a, fr *sc) {
   if (threadIdx.x < PP_GATE_NS) sc[threadIdx.x] = ldg_fr(a.s[threadIdx.x]);
   __syncthreads();
   if (threadIdx.x == 0)
     sc[PP_GATE_NS] =
         fr_mul(fr_mul(sc[PP_GATE_S_THREE], sc[PP_GATE_S_ONE]), sc[PP_GATE_S_TWO]);
   __syncthreads();
+}
+
 #define S(name) sc[PP_GATE_S_##name]
 #define V(name) ldcs_fr(a.v[PP_GATE_V_##name] + i)
+
+__global__ void __launch_bounds__(kThreads, 2) k_gate_range_logic(const GateArgs a, fr *out,
+                                                               uint64_t n) {
+  __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
+  stage_scalars(a, sc);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const fr k312 = sc[PP_GATE_NS];
-    const fr a_ = V(A), b = V(B), c = V(C), d = V(D), an = V(A_NEXT), bn = V(B_NEXT),
-             dn = V(D_NEXT);
+    const fr a_ = V(A), b = V(B), c = V(C), d = V(D), dn = V(D_NEXT);
     const fr four = S(FOUR);
     const fr a4 = fr_mul(a_, four), b4 = fr_mul(b, four), c4 = fr_mul(c, four),
              d4 = fr_mul(d, four);
@@ -114,51 +132,64 @@ __global__ void __launch_bounds__(kThreads) k_gate_constraint(const GateArgs a, 
     fr acc = fr_mul(fr_mul(t, S(RANGE_CHALLENGE)), V(RANGE));
 
     // logic gate
-    {
-      const fr da = fr_sub(a4, an), db = fr_sub(b4, bn);
-      const fr w = fr_add(da, db), e = fr_sub(dn, d4);
-      const fr da2 = fr_mul(da, da);
-      const fr inner =
-          fr_sub(fr_mul(w, S(EIGHTYONE)),
-                 fr_add(fr_mul(c, fr_mul(fr_sub(c4, fr_mul(w, S(EIGHTEEN))), S(EIGHTYONE))),
-                        fr_mul(fr_add(da2, da2), S(EIGHTEEN))));
-      const fr A = fr_sub(fr_mul(fr_add(e, w), S(THREE)),
-                          fr_mul(fr_mul(c, fr_mul(inner, S(EIGHTYTHREE))), S(TWO)));
-      const fr B = fr_mul(V(Q_C), fr_sub(fr_mul(e, S(NINE)), fr_mul(w, S(THREE))));
-      fr l = fr_mul(fr_add(A, B), S(KAPPA_QU_LOGIC));
-      l = fr_add(l, fr_mul(fr_sub(c, fr_mul(da, db)), S(KAPPA_CU_LOGIC)));
-      l = fr_add(l, delta4(e, k312));
-      l = fr_add(l, fr_mul(fr_mul(da2, da2), k312));
-      l = fr_add(l, delta4(db, k312));
-      acc = fr_add(acc, fr_mul(fr_mul(l, S(LOGIC_CHALLENGE)), V(LOGIC)));
-    }
+    const fr da = fr_sub(a4, V(A_NEXT)), db = fr_sub(b4, V(B_NEXT));
+    const fr w = fr_add(da, db), e = fr_sub(dn, d4);
+    const fr da2 = fr_mul(da, da);
+    const fr inner =
+        fr_sub(fr_mul(w, S(EIGHTYONE)),
+               fr_add(fr_mul(c, fr_mul(fr_sub(c4, fr_mul(w, S(EIGHTEEN))), S(EIGHTYONE))),
+                      fr_mul(fr_add(da2, da2), S(EIGHTEEN))));
+    const fr A = fr_sub(fr_mul(fr_add(e, w), S(THREE)),
+                        fr_mul(fr_mul(c, fr_mul(inner, S(EIGHTYTHREE))), S(TWO)));
+    const fr B = fr_mul(V(Q_C), fr_sub(fr_mul(e, S(NINE)), fr_mul(w, S(THREE))));
+    fr l = fr_mul(fr_add(A, B), S(KAPPA_QU_LOGIC));
+    l = fr_add(l, fr_mul(fr_sub(c, fr_mul(da, db)), S(KAPPA_CU_LOGIC)));
+    l = fr_add(l, delta4(e, k312));
+    l = fr_add(l, fr_mul(fr_mul(da2, da2), k312));
+    l = fr_add(l, delta4(db, k312));
+    acc = fr_add(acc, fr_mul(fr_mul(l, S(LOGIC_CHALLENGE)), V(LOGIC)));
+    st_fr(out + i, acc);
+  }
+}
 
+__global__ void __launch_bounds__(kThreads, 2) k_gate_arith(const GateArgs a, fr *out, uint64_t n) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const fr a_ = V(A), b = V(B), c = V(C), d = V(D);
     // arithmetic gate (with the x^alpha S-box terms) and public inputs
-    const fr ab = fr_mul(a_, b);
-    {
-      fr ar = fr_mul(fr_pow_u64(d, a.sbox_alpha), V(Q_H4));
-      ar = fr_add(ar, fr_mul(fr_pow_u64(b, a.sbox_alpha), V(Q_HR)));
-      ar = fr_add(ar, fr_mul(fr_pow_u64(a_, a.sbox_alpha), V(Q_HL)));
-      ar = fr_add(ar, fr_mul(d, V(Q_4)));
-      ar = fr_add(ar, fr_mul(c, V(Q_O)));
-      ar = fr_add(ar, fr_mul(b, V(Q_R)));
-      ar = fr_add(ar, fr_mul(ab, V(Q_M)));
-      ar = fr_add(ar, fr_mul(a_, V(Q_L)));
-      ar = fr_add(ar, V(Q_C));
-      acc = fr_add(acc, fr_mul(ar, V(Q_ARITH)));
-      acc = fr_add(acc, V(PI));
-    }
+    fr ar = fr_mul(pow_small(d, a.sbox_alpha), V(Q_H4));
+    ar = fr_add(ar, fr_mul(pow_small(b, a.sbox_alpha), V(Q_HR)));
+    ar = fr_add(ar, fr_mul(pow_small(a_, a.sbox_alpha), V(Q_HL)));
+    ar = fr_add(ar, fr_mul(d, V(Q_4)));
+    ar = fr_add(ar, fr_mul(c, V(Q_O)));
+    ar = fr_add(ar, fr_mul(b, V(Q_R)));
+    ar = fr_add(ar, fr_mul(fr_mul(a_, b), V(Q_M)));
+    ar = fr_add(ar, fr_mul(a_, V(Q_L)));
+    ar = fr_add(ar, V(Q_C));
+    const fr acc = fr_add(fr_add(ld_fr(out + i), fr_mul(ar, V(Q_ARITH))), V(PI));
+    st_fr(out + i, acc);
+  }
+}
 
+__global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a, fr *out, uint64_t n) {
+  __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
+  stage_scalars(a, sc);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const fr a_ = V(A), b = V(B), c = V(C), d = V(D);
+    const fr an = V(A_NEXT), bn = V(B_NEXT), dn = V(D_NEXT);
+    const fr pd = S(P_D);
+    const fr bc = fr_mul(b, c);
     // fixed-base group addition
+    fr f;
     {
-      const fr one = S(ONE), pd = S(P_D);
-      const fr qc = V(Q_C), qr = V(Q_R), ql = V(Q_L);
-      const fr abc = fr_mul(ab, c);
+      const fr one = S(ONE);
+      const fr abc = fr_mul(a_, bc);
       const fr one2 = fr_mul(one, one);
       const fr dn2 = fr_mul(dn, dn);
-      const fr qr2 = fr_mul(fr_mul(qr, dn2), one2);
-      const fr qldn = fr_mul(ql, dn);
-      fr f = fr_mul(fr_sub(c, fr_mul(qc, dn)), S(KAPPA_FB));
+      const fr qr2 = fr_mul(fr_mul(V(Q_R), dn2), one2);
+      const fr qldn = fr_mul(V(Q_L), dn);
+      f = fr_mul(fr_sub(c, fr_mul(V(Q_C), dn)), S(KAPPA_FB));
       f = fr_add(f, fr_mul(fr_sub(fr_sub(bn, fr_mul(fr_mul(abc, bn), pd)),
                                   fr_sub(fr_mul(b, qr2), fr_mul(a_, fr_mul(qldn, S(P_A))))),
                            S(KAPPA_CU_FB)));
@@ -166,26 +197,20 @@ __global__ void __launch_bounds__(kThreads) k_gate_constraint(const GateArgs a, 
       f = fr_add(f, fr_mul(fr_sub(fr_add(an, fr_mul(fr_mul(abc, an), pd)),
                                   fr_add(fr_mul(b, qldn), fr_mul(a_, qr2))),
                            S(KAPPA_SQ_FB)));
-      acc = fr_add(acc, fr_mul(fr_mul(f, S(FB_CHALLENGE)), V(FIXED_GROUP_ADD)));
+      f = fr_mul(fr_mul(f, S(FB_CHALLENGE)), V(FIXED_GROUP_ADD));
     }
-
     // variable-base group addition
-    {
-      const fr pd = S(P_D);
-      const fr bc = fr_mul(b, c);
-      fr v1 = fr_sub(fr_sub(fr_mul(b, d), fr_mul(fr_mul(a_, c), S(P_A))),
-                     fr_sub(bn, fr_mul(bc, fr_mul(dn, fr_mul(bn, pd)))));
-      v1 = fr_mul(v1, S(KAPPA_SQ_VB));
-      fr v2 = fr_sub(fr_add(dn, bc), fr_add(an, fr_mul(bc, fr_mul(dn, fr_mul(an, pd)))));
-      v2 = fr_add(fr_sub(dn, fr_mul(a_, d)), fr_mul(v2, S(KAPPA_VB)));
-      acc = fr_add(acc,
-                   fr_mul(fr_mul(fr_add(v1, v2), S(VB_CHALLENGE)), V(VARIABLE_GROUP_ADD)));
-    }
-    st_fr(out + i, acc);
+    fr v1 = fr_sub(fr_sub(fr_mul(b, d), fr_mul(fr_mul(a_, c), S(P_A))),
+                   fr_sub(bn, fr_mul(bc, fr_mul(dn, fr_mul(bn, pd)))));
+    v1 = fr_mul(v1, S(KAPPA_SQ_VB));
+    fr v2 = fr_sub(fr_add(dn, bc), fr_add(an, fr_mul(bc, fr_mul(dn, fr_mul(an, pd)))));
+    v2 = fr_add(fr_sub(dn, fr_mul(a_, d)), fr_mul(v2, S(KAPPA_VB)));
+    const fr vb = fr_mul(fr_mul(fr_add(v1, v2), S(VB_CHALLENGE)), V(VARIABLE_GROUP_ADD));
+    st_fr(out + i, fr_add(fr_add(ld_fr(out + i), f), vb));
   }
+}
 #undef S
 #undef V
-}
 
 bool aligned16(const void *p) { return p && (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
@@ -297,8 +322,17 @@ extern "C" int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n
     }
     g.s[j] = static_cast<const pp::fr *>(a->s[j]);
   }
-  g.sbox_alpha = (uint64_t)a->sbox_alpha;
-  pp::k_gate_constraint<<<pp::grid_for(n), pp::kThreads, 0, (cudaStream_t)stream>>>(
+  g.sbox_alpha = (uint32_t)a->sbox_alpha;
+  const unsigned grid = pp::grid_for(n);
+  pp::k_gate_range_logic<<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+      g, static_cast<pp::fr *>(d_out), n);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gate_arith<<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+      g, static_cast<pp::fr *>(d_out), n);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gate_groups<<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
       g, static_cast<pp::fr *>(d_out), n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();

@@ -18,6 +18,9 @@
 //       inputs <dir>/<argument name>.bin -> <dir>/quotient_out.bin
 //   pp_compat_driver gate <n> <sbox_alpha> <dir>
 //       compute_gate_constraint_allmerge_cuda -> <dir>/gate_out.bin
+//   pp_compat_driver convert <n> <in.bin> <outdir>
+//       read_file, to_base -> base.bin and base.txt (writeToFile), to_mont of
+//       that -> mont.bin (the input again)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -25,6 +28,7 @@
 #include <vector>
 
 #include "function.h"
+#include "io.h"
 #include "zksnark.h"
 
 static std::vector<unsigned char> read_file(const std::string &path, size_t bytes) {
@@ -154,12 +158,27 @@ static int gate(size_t n, long long alpha, const std::string &dir) {
   return 0;
 }
 
+static int convert(size_t n, const std::string &in, const std::string &outdir) {
+  SyncedMemory x(n * 32);
+  ::read_file(in.c_str(), x.mutable_cpu_data());
+  SyncedMemory base = to_base(x);
+  SyncedMemory mont = to_mont(base);
+  cudaDeviceSynchronize();
+  write_file(outdir + "/base.bin", base.mutable_cpu_data(), n * 32);
+  writeToFile(outdir + "/base.txt", static_cast<uint64_t *>(base.mutable_cpu_data()), 4 * n);
+  write_file(outdir + "/mont.bin", mont.mutable_cpu_data(), n * 32);
+  std::printf("convert ok\n");
+  return 0;
+}
+
 int main(int argc, char **argv) {
   try {
     if (argc >= 5 && std::string(argv[1]) == "miss_ops") return miss_ops(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 5 && std::string(argv[1]) == "ntt") return ntt_check(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 4 && std::string(argv[1]) == "quotient")
       return quotient(std::strtoull(argv[2], nullptr, 10), argv[3]);
+    if (argc >= 5 && std::string(argv[1]) == "convert")
+      return convert(std::strtoull(argv[2], nullptr, 10), argv[3], argv[4]);
     if (argc >= 5 && std::string(argv[1]) == "gate")
       return gate(std::strtoull(argv[2], nullptr, 10), std::atoll(argv[3]), argv[4]);
     if (argc >= 6 && std::string(argv[1]) == "lde")
@@ -169,6 +188,6 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
     return 3;
   }
-  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate ...\n", argv[0]);
+  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate|convert ...\n", argv[0]);
   return 1;
 }

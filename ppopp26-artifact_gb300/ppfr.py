@@ -42,6 +42,9 @@ def lib():
                 "pp_ntt": [v, v, u32, i, v],
                 "pp_lde": [v, v, u32, u32, u32, v],
                 "pp_ntt_host": [v, v, u32, i, v],
+                "pp_to_mont": [v, v, u64, v],
+                "pp_to_base": [v, v, u64, v],
+                "pp_count_noncanonical": [v, u64, v, v],
                 "pp_lde_host": [v, v, u32, u32, u32, v],
                 "pp_gp_prefix": [v, u64, v],
                 "pp_gp_perm": [v, v, v, v, u32, v],
@@ -161,6 +164,47 @@ def lde_host(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):
         out = empty_pinned(x.shape[0] << lam)
     check(lib().pp_lde_host(_hptr(x), _hptr(out), lg, lam, mode, _stream(stream)))
     return out
+
+
+# -------------------------------------------------------------- data formats
+def read_raw(path: str, n: int = None, pinned: bool = True):
+    """Raw file of 32-byte little-endian Montgomery elements (the reference's
+    input.bin format) -> (n, 4) int64 host tensor, page-locked by default."""
+    torch = _torch()
+    import numpy as np
+    a = np.fromfile(path, dtype=np.int64, count=-1 if n is None else 4 * n)
+    if a.size % 4 or (n is not None and a.size != 4 * n):
+        raise ValueError("%s: expected %s whole 32-byte elements" % (path, n if n is not None else "only"))
+    t = torch.empty((a.size // 4, 4), dtype=torch.int64, pin_memory=pinned)
+    t.copy_(torch.from_numpy(a.reshape(-1, 4)))
+    return t
+
+
+def write_raw(path: str, t) -> None:
+    """(n, 4) int64 tensor (host or device) -> raw 32-byte element file."""
+    t.detach().cpu().contiguous().numpy().tofile(path)
+
+
+def to_mont(x, out=None, stream=None):
+    """pp_to_mont: a -> a R mod r."""
+    out = empty(x.shape[0], x.device) if out is None else out
+    check(lib().pp_to_mont(_ptr(x), _ptr(out), x.shape[0], _stream(stream)))
+    return out
+
+
+def to_base(x, out=None, stream=None):
+    """pp_to_base: a -> a R^-1 mod r."""
+    out = empty(x.shape[0], x.device) if out is None else out
+    check(lib().pp_to_base(_ptr(x), _ptr(out), x.shape[0], _stream(stream)))
+    return out
+
+
+def count_noncanonical(x, stream=None) -> int:
+    """Number of elements >= r (synchronises the stream to read the count)."""
+    torch = _torch()
+    c = torch.zeros(1, dtype=torch.int64, device=x.device)
+    check(lib().pp_count_noncanonical(_ptr(x), x.shape[0], ctypes.c_void_p(c.data_ptr()), _stream(stream)))
+    return int(c.item())
 
 
 # ------------------------------------------------------ quotient constraints
