@@ -79,6 +79,7 @@ def lib():
                 "or_quotient_copy": [v, v, v, v, v, v, v, v, u],
                 "or_quotient_term_one": [v, v, v, v, u],
                 "or_gate_constraint": [v, v, ctypes.c_int64, v, u],
+                "or_g1_msm": [v, v, u, v, i], "or_g1_mul_gen": [v, u, v, i], "or_g1_add": [v, v, v],
             }
             for name, args in sigs.items():
                 fn = getattr(L, name)
@@ -351,4 +352,32 @@ def gate_constraint(vectors: dict, scalars: dict, sbox_alpha: int) -> np.ndarray
     out = empty(n)
     lib().or_gate_constraint(ctypes.cast(vp, ctypes.c_void_p), ctypes.cast(sp, ctypes.c_void_p),
                              int(sbox_alpha), out.ctypes.data, n)
+    return out
+
+
+# ------------------------------------------------------------------------ G1
+def g1_mul_gen(scalars, nthreads: int = 0) -> np.ndarray:
+    """scalars (n, 4) -> affine points (n, 12): s_i * G."""
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    out = np.empty((s.shape[0], 12), dtype=np.uint64)
+    lib().or_g1_mul_gen(s.ctypes.data, s.shape[0], out.ctypes.data, nthreads)
+    return out
+
+
+def g1_msm(points, scalars, nthreads: int = 0) -> np.ndarray:
+    """sum_i scalars[i] * points[i] -> affine (12,)."""
+    p = np.ascontiguousarray(points, dtype=np.uint64).reshape(-1, 12)
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    assert p.shape[0] == s.shape[0]
+    out = np.empty(12, dtype=np.uint64)
+    lib().or_g1_msm(p.ctypes.data if p.size else None, s.ctypes.data if s.size else None, p.shape[0],
+                    out.ctypes.data, nthreads)
+    return out
+
+
+def g1_add(a, b) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(12)
+    b = np.ascontiguousarray(b, dtype=np.uint64).reshape(12)
+    out = np.empty(12, dtype=np.uint64)
+    lib().or_g1_add(a.ctypes.data, b.ctypes.data, out.ctypes.data)
     return out

@@ -67,6 +67,16 @@ void or_quotient_term_one(const uint64_t *z, const uint64_t *l1, const uint64_t 
 void or_gate_constraint(const uint64_t *const v[22], const uint64_t *const s[24], int64_t sbox_alpha,
                         uint64_t *out, uint64_t n);
 
+/* BLS12-381 G1 (pp_oracle_g1.c).  Affine points are 12 uint64 (x, y in
+ * Montgomery form over Fq, R = 2^384; all zero = infinity); scalars 4 uint64
+ * read as plain integers.  or_g1_msm: sum_i s_i P_i (PLONK/utils/function.cu:
+ * 395-411 multi_scalar_mult); or_g1_mul_gen: s_i G for the standard
+ * generator; or_g1_add: a + b.  nthreads <= 0 uses all. */
+void or_g1_msm(const uint64_t *points, const uint64_t *scalars, uint64_t n, uint64_t out[12],
+               int nthreads);
+void or_g1_mul_gen(const uint64_t *scalars, uint64_t n, uint64_t *out, int nthreads);
+void or_g1_add(const uint64_t a[12], const uint64_t b[12], uint64_t out[12]);
+
 /* bit-exact byte comparison helper: index of first differing element or -1 */
 int64_t or_first_diff(const uint64_t *a, const uint64_t *b, uint64_t n);
 
