@@ -1,0 +1,230 @@
+// fq.cuh -- BLS12-381 base field Fq (381-bit) for the G1 multi-scalar
+// multiplication: Montgomery form with R = 2^384, canonical (< q), 12 x
+// 32-bit little-endian limbs -- the same bytes as the reference's 6 x 64-bit
+// limbs (PLONK/utils/mont/cuda/ff/bls12-381.hpp BLS12_381_P, BLS12_381_RR,
+// one).  Usable on host and device (the carry primitives of fr.cuh are
+// emulated on the host), so the formulas are unit-tested on the CPU.
+#pragma once
+#include "fr.cuh"
+
+namespace pp {
+
+struct fq {
+  uint32_t v[12];
+};
+
+// q, least significant limb first
+#define PP_Q0 0xffffaaabu
+#define PP_Q1 0xb9feffffu
+#define PP_Q2 0xb153ffffu
+#define PP_Q3 0x1eabfffeu
+#define PP_Q4 0xf6b0f624u
+#define PP_Q5 0x6730d2a0u
+#define PP_Q6 0xf38512bfu
+#define PP_Q7 0x64774b84u
+#define PP_Q8 0x434bacd7u
+#define PP_Q9 0x4b1ba7b6u
+#define PP_Q10 0x397fe69au
+#define PP_Q11 0x1a0111eau
+#define PP_QP 0xfffcfffdu  // -q^-1 mod 2^32
+
+PP_HD fq fq_zero() {
+  fq r;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) r.v[i] = 0;
+  return r;
+}
+
+// R mod q: the Montgomery form of 1
+PP_HD fq fq_one() {
+  return fq{{0x0002fffdu, 0x76090000u, 0xc40c0002u, 0xebf4000bu, 0x53c758bau, 0x5f489857u,
+             0x70525745u, 0x77ce5853u, 0xa256ec6du, 0x5c071a97u, 0xfa80e493u, 0x15f65ec3u}};
+}
+
+PP_HD bool fq_is_zero(const fq &a) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) o |= a.v[i];
+  return o == 0;
+}
+
+PP_HD bool fq_eq(const fq &a, const fq &b) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) o |= a.v[i] ^ b.v[i];
+  return o == 0;
+}
+
+// x - q if x >= q (x < 2q), branch-free selection
+PP_HD void fq_reduce_once(uint32_t x[12]) {
+  const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                          PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  uint32_t d[12];
+  d[0] = sub_cc(x[0], q[0]);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) d[i] = subc_cc(x[i], q[i]);
+  const uint32_t borrow = subc(0, 0);  // all ones when x < q
+#pragma unroll
+  for (int i = 0; i < 12; ++i) x[i] = borrow ? x[i] : d[i];
+}
+
+PP_HD fq fq_add(const fq &a, const fq &b) {
+  fq r;
+  r.v[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) r.v[i] = addc_cc(a.v[i], b.v[i]);
+  // a + b < 2q < 2^383: no carry out of the top limb
+  fq_reduce_once(r.v);
+  return r;
+}
+
+PP_HD fq fq_sub(const fq &a, const fq &b) {
+  const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                          PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  fq r;
+  r.v[0] = sub_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) r.v[i] = subc_cc(a.v[i], b.v[i]);
+  const uint32_t borrow = subc(0, 0);
+  r.v[0] = add_cc(r.v[0], q[0] & borrow);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) r.v[i] = addc_cc(r.v[i], q[i] & borrow);
+  return r;
+}
+
+PP_HD fq fq_dbl(const fq &a) { return fq_add(a, a); }
+
+PP_HD fq fq_neg(const fq &a) { return fq_sub(fq_zero(), a); }
+
+// Montgomery product a b R^-1 mod q: CIOS with the rows of Fr's variant 9
+// (independent wide products per row, one add chain), m_i = t_0 * q' per row.
+PP_HD void fq_row_ab(uint32_t t[14], uint32_t ai, const uint32_t b[12]) {
+  uint32_t lo[12], hi[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) {
+    const uint64_t s = (uint64_t)ai * b[j] + t[j];
+    lo[j] = (uint32_t)s;
+    hi[j] = (uint32_t)(s >> 32);
+  }
+  t[0] = lo[0];
+  t[1] = add_cc(lo[1], hi[0]);
+#pragma unroll
+  for (int j = 2; j < 12; ++j) t[j] = addc_cc(lo[j], hi[j - 1]);
+  t[12] = addc_cc(t[12], hi[11]);
+  t[13] = addc(t[13], 0);
+}
+
+PP_HD void fq_row_red(uint32_t t[14]) {
+  const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                          PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  const uint32_t m = t[0] * PP_QP;
+  uint32_t lo[12], hi[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) {
+    const uint64_t s = (uint64_t)m * q[j] + t[j];
+    lo[j] = (uint32_t)s;
+    hi[j] = (uint32_t)(s >> 32);
+  }
+  // lo[0] = 0 by the choice of m; word j+1 collects lo[j+1] + hi[j]
+  uint32_t u[13];
+  u[0] = add_cc(lo[1], hi[0]);
+#pragma unroll
+  for (int j = 1; j < 11; ++j) u[j] = addc_cc(lo[j + 1], hi[j]);
+  u[11] = addc_cc(t[12], hi[11]);
+  u[12] = addc(t[13], 0);
+#pragma unroll
+  for (int j = 0; j < 13; ++j) t[j] = u[j];
+  t[13] = 0;
+}
+
+PP_HD fq fq_mul(const fq &a, const fq &b) {
+  uint32_t t[14];
+#pragma unroll
+  for (int j = 0; j < 14; ++j) t[j] = 0;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    fq_row_ab(t, a.v[i], b.v);
+    fq_row_red(t);
+  }
+  // t < 2q < 2^383: t[12] = 0
+  fq_reduce_once(t);
+  fq r;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) r.v[i] = t[i];
+  return r;
+}
+
+PP_HD fq fq_sqr(const fq &a) { return fq_mul(a, a); }
+
+// ---- binary extended-GCD inverse: shifts and subtractions instead of the
+// ~480 dependent multiplies of a Fermat chain (for single-thread use)
+PP_HD bool fq_words_is_one(const uint32_t a[12]) {
+  uint32_t o = a[0] ^ 1u;
+#pragma unroll
+  for (int i = 1; i < 12; ++i) o |= a[i];
+  return o == 0;
+}
+PP_HD bool fq_words_lt(const uint32_t a[12], const uint32_t b[12]) {
+  for (int i = 11; i >= 0; --i)
+    if (a[i] != b[i]) return a[i] < b[i];
+  return false;
+}
+PP_HD void fq_words_shr1(uint32_t a[12]) {
+#pragma unroll
+  for (int i = 0; i < 11; ++i) a[i] = (a[i] >> 1) | (a[i + 1] << 31);
+  a[11] >>= 1;
+}
+PP_HD void fq_words_sub(uint32_t a[12], const uint32_t b[12]) {
+  a[0] = sub_cc(a[0], b[0]);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) a[i] = subc_cc(a[i], b[i]);
+}
+// x / 2 mod q for x < q: (x + q) / 2 when x is odd (x + q < 2^383)
+PP_HD void fq_half(uint32_t x[12]) {
+  const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                          PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  const uint32_t mask = 0u - (x[0] & 1u);
+  x[0] = add_cc(x[0], q[0] & mask);
+#pragma unroll
+  for (int i = 1; i < 12; ++i) x[i] = addc_cc(x[i], q[i] & mask);
+  fq_words_shr1(x);
+}
+
+// a^-1 in Montgomery form (0 -> 0).  The GCD inverts the raw word value
+// A = a R; the result A^-1 times R^3 under one Montgomery multiply is
+// a^-1 R.
+PP_HD fq fq_inv(const fq &a) {
+  if (fq_is_zero(a)) return fq_zero();
+  uint32_t u[12], v[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                           PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  fq x1 = fq_zero(), x2 = fq_zero();
+  x1.v[0] = 1;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) u[i] = a.v[i];
+  // at most ~2 * 384 halvings and 384 subtractions for canonical input; the
+  // bounds only guard against non-canonical input
+  for (int guard = 0; guard < 1536 && !fq_words_is_one(u) && !fq_words_is_one(v); ++guard) {
+    for (int k = 0; k < 384 && !(u[0] & 1u); ++k) {
+      fq_words_shr1(u);
+      fq_half(x1.v);
+    }
+    for (int k = 0; k < 384 && !(v[0] & 1u); ++k) {
+      fq_words_shr1(v);
+      fq_half(x2.v);
+    }
+    if (!fq_words_lt(u, v)) {
+      fq_words_sub(u, v);
+      x1 = fq_sub(x1, x2);
+    } else {
+      fq_words_sub(v, u);
+      x2 = fq_sub(x2, x1);
+    }
+  }
+  const fq y = fq_words_is_one(u) ? x1 : x2;
+  // R^3 mod q
+  const fq r3 = {{0xd94ca1e0u, 0xed48ac6bu, 0x03a7adf8u, 0x315f831eu, 0x615e29ddu, 0x9a53352au,
+                  0x921e1761u, 0x34c04e5eu, 0x65724728u, 0x2512d435u, 0x91755d4du, 0x0aa63460u}};
+  return fq_mul(y, r3);
+}
+
+}  // namespace pp
