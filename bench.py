@@ -402,6 +402,7 @@ def secondary_ops(pp, torch):
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
     del w, s, p
     constraint_bench(pp, torch, rate, res)
+    msm_bench(pp, torch, rate, res)
     res["batched"] = batched_bench(pp, torch)
     res["serving"] = serving_bench(pp, torch)
     return res
@@ -442,6 +443,35 @@ def constraint_bench(pp, torch, rate, res):
     for k, mm in (("quotient_permutation_2^22", 18), ("gate_constraint_2^22", 104)):
         pts = res[k]["Melem_per_s"] * 1e6
         res[k]["int_frac_of_nominal_peak"] = round(pts * mm * 256 / peak, 4)
+
+
+def msm_bench(pp, torch, rate, res):
+    """G1 multi-scalar multiplication of 2^20 points.  The points are 1024
+    distinct multiples of the generator (made by the oracle on the host, a
+    set-up step outside the timed region) repeated 1024 times; the scalars are
+    seeded random canonical Fr values.  The bucket method's work does not
+    depend on repeated points.  Integer fraction: W n mixed additions of ~10
+    Fq Montgomery multiplies (W = 256 / c + 1 windows), each 4 * 12^2 = 576
+    32-bit multiply instructions, against the nominal integer peak."""
+    import numpy as np
+    from oracle import oracle as O
+
+    ppfr = pp.ppfr
+    n = 1 << 20
+    base = O.g1_mul_gen(O.random_fr(1024, 77))
+    pts = torch.from_numpy(np.ascontiguousarray(np.tile(base, (n // 1024, 1))).view(np.int64)).cuda()
+    sc = ppfr.random_fr(n, 5)
+    out = torch.empty((3, 6), dtype=torch.int64, device="cuda")
+    name = "msm_g1_2^20"
+    rate(name, lambda: ppfr.msm_g1(pts, sc, out=out), n, 3)
+    c = ppfr.msm_window_bits(n)
+    windows = 256 // c + 1
+    sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6
+    instr = windows * n * 10 * 576
+    res[name].update({"window_bits": c, "windows": windows,
+                      "int_frac_of_nominal_peak": round(instr / (res[name]["ms"] / 1e3) / peak, 4),
+                      "points": "1024 distinct generator multiples, tiled"})
 
 
 def batched_bench(pp, torch):

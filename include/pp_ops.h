@@ -303,6 +303,24 @@ typedef struct {
 } pp_gate_args;
 int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n, void *stream);
 
+/* ------------------------------------------- G1 multi-scalar multiply ---
+ * d_out = sum_i s_i P_i over BLS12-381 G1 (y^2 = x^3 + 4 over Fq).
+ *  d_points: n affine points (x, y), each coordinate 6 little-endian 64-bit
+ *    limbs in Montgomery form (R = 2^384, canonical), 96 bytes per point; an
+ *    all-zero point is infinity and contributes nothing.
+ *  d_scalars: n scalars of 4 little-endian 64-bit limbs, read as plain
+ *    integers (no Montgomery decoding), as the reference's MSM does.
+ *  d_out: one Jacobian point (X, Y, Z), 144 bytes, normalised to Z = 1
+ *    (Montgomery form) -- the affine result -- or all zero for infinity.
+ * Replaces multi_scalar_mult (PLONK/utils/function.cu:395-411) ->
+ * cuda::msm_zkp_cuda (PLONK/utils/zkp/cuda/zksnark_msm.cu:48-88) and
+ * cpu::msm_collect_cpu (PLONK/utils/zkp/cpu/msmcollect.cpp:5-41); the final
+ * window aggregation runs on the GPU.  n < 2^31.  Uses a per-stream device
+ * workspace of about 32 W n + 230 W 2^(c-1) bytes (c = window bits, W =
+ * 256 / c + 1 windows; pp_msm_g1_window_bits gives c). */
+int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n, void *d_out, void *stream);
+int pp_msm_g1_window_bits(uint64_t n);
+
 /* -------------------------------------------------------- data formats ---
  * The reference's element files are raw 32-byte little-endian Montgomery
  * elements (read_file miss_ops.cu:8-24, read_file_exact lde.cu:222-231);

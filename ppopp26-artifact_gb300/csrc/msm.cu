@@ -1,0 +1,600 @@
+// msm.cu -- BLS12-381 G1 multi-scalar multiplication sum_i s_i P_i on the
+// GPU (Pippenger's bucket method with signed digits).
+//
+// Replaces multi_scalar_mult (PLONK/utils/function.cu:395-411) ->
+// cuda::msm_zkp_cuda (PLONK/utils/zkp/cuda/zksnark_msm.cu:48-88, sppark's
+// Pippenger with mont = false) + cpu::msm_collect_cpu (zkp/cpu/
+// msmcollect.cpp): same inputs (affine points over Fq in Montgomery form,
+// scalars as plain 256-bit integers), one Jacobian point out, with the final
+// aggregation on the GPU instead of the host.
+//
+// Pipeline (all on one stream, workspace slot 3):
+//   1. digits    one thread per scalar: c-bit windows recoded to signed
+//                digits in [-2^(c-1), 2^(c-1)], bucket |d| - 1 per window
+//                (W = floor(256 / c) + 1 windows, so any 256-bit scalar is
+//                exact); bucket sizes counted with warp-aggregated atomics
+//   2. scan      exclusive prefix sum of the W * 2^(c-1) bucket sizes (tiled)
+//   3. scatter   (point index, sign) into each bucket's slice: a counting sort
+//   4. buckets   bucket sums in groups of at most K points per thread, then
+//                levels of groups of K partial sums for buckets that had more
+//                (a bucket can hold up to all n points: equal scalars, or the
+//                few-bit top window), so no thread sums more than K values
+//   5. segments  one thread per run of G buckets: running sums T = sum
+//                (j + 1) B and R = sum B over its run
+//   6. windows   one block per window: sum T + G sum s R_s, the index weights
+//                merged up a tree with power-of-two doublings
+//   7. final     one warp: Horner over the windows (c doublings each, the
+//                independent multiplies of each step on different lanes), one
+//                inversion to affine
+// Every step is integer-multiply bound (an Fq multiply is ~300 32-bit wide
+// products) except the sort, which is a few bytes per point and window.
+#include <cstring>
+
+#include "common.cuh"
+#include "g1.cuh"
+
+namespace pp {
+namespace {
+
+constexpr uint32_t kNone = 0xffffffffu;
+
+struct MsmPlan {
+  uint32_t c;  // window bits
+  uint32_t W;  // windows: W c >= 257, so the top window's carry has a home
+  uint32_t B;  // buckets per window, 2^(c-1)
+  uint32_t G;  // buckets per aggregation segment
+  uint32_t S;  // segments per window, B / G
+};
+
+// minimise W (10 n + 14 2^c) Fq multiplies: the bucket sums (one mixed add
+// per point and window) against the aggregation (two adds per bucket)
+MsmPlan msm_plan(uint64_t n) {
+  MsmPlan p{};
+  double best = 0;
+  for (uint32_t c = 6; c <= 20; ++c) {
+    const double W = 256 / c + 1;
+    const double cost = W * (10.0 * (double)n + 14.0 * (double)(1u << c));
+    if (p.c == 0 || cost < best) {
+      best = cost;
+      p.c = c;
+    }
+  }
+  p.W = 256 / p.c + 1;
+  p.B = 1u << (p.c - 1);
+  p.G = p.B < 32 ? p.B : 32;
+  p.S = p.B / p.G;
+  return p;
+}
+
+__device__ __forceinline__ g1a ld_g1a(const g1a *p) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(p);
+  g1a r;
+  uint32_t *w = reinterpret_cast<uint32_t *>(&r);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const uint4 u = __ldg(q + k);
+    w[4 * k] = u.x;
+    w[4 * k + 1] = u.y;
+    w[4 * k + 2] = u.z;
+    w[4 * k + 3] = u.w;
+  }
+  return r;
+}
+
+// bits [off, off + c) of a 256-bit scalar (8 little-endian words), c <= 20
+__device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], uint32_t off, uint32_t c) {
+  const uint32_t w = off >> 5, sh = off & 31;
+  if (w >= 8) return 0;
+  uint64_t x = s[w];
+  if (w + 1 < 8) x |= (uint64_t)s[w + 1] << 32;
+  return (uint32_t)(x >> sh) & ((1u << c) - 1);
+}
+
+// atomicAdd(base + key, 1) for every active lane, one atomic per distinct key
+// in the warp; returns the old value plus the lane's rank among equal keys
+__device__ __forceinline__ uint32_t warp_increment(uint32_t *base, uint32_t key) {
+  const uint32_t mask = __activemask();
+  const uint32_t same = __match_any_sync(mask, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(same) - 1;
+  uint32_t old = 0;
+  if (lane == leader) old = atomicAdd(base + key, (uint32_t)__popc(same));
+  old = __shfl_sync(same, old, leader);
+  return old + __popc(same & ((1u << lane) - 1));
+}
+
+__global__ void k_msm_digits(const uint32_t *__restrict__ scalars, uint64_t n, MsmPlan p,
+                             uint32_t *__restrict__ digits, uint32_t *__restrict__ counts) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t s[8];
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(scalars) + 2 * i);
+    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(scalars) + 2 * i + 1);
+    s[0] = a.x, s[1] = a.y, s[2] = a.z, s[3] = a.w, s[4] = b.x, s[5] = b.y, s[6] = b.z, s[7] = b.w;
+    uint32_t carry = 0;
+    for (uint32_t w = 0; w < p.W; ++w) {
+      const uint32_t raw = window_bits(s, w * p.c, p.c) + carry;
+      uint32_t mag, sign;
+      if (raw > p.B) {  // d = raw - 2^c < 0
+        mag = (1u << p.c) - raw;
+        sign = 1;
+        carry = 1;
+      } else {
+        mag = raw;
+        sign = 0;
+        carry = 0;
+      }
+      uint32_t e = kNone;
+      if (mag) {
+        const uint32_t bucket = mag - 1;
+        e = (bucket << 1) | sign;
+        warp_increment(counts, w * p.B + bucket);
+      }
+      digits[(uint64_t)w * n + i] = e;
+    }
+  }
+}
+
+// Exclusive prefix sum of len counts into out (len + 1 entries: the last is
+// the total) and, when cursor is not null, a copy of it.  Three launches over
+// tiles of 4096 entries: tile sums, a scan of the tile sums, tile scans.
+constexpr int kScanThreads = 256, kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_sum[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kScanThreads / 32 ? warp_sum[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
+      if (lane >= d) w += y;
+    }
+    if (lane < kScanThreads / 32) warp_sum[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t before = (warp ? warp_sum[warp - 1] : 0) + x - v;
+  *total = warp_sum[kScanThreads / 32 - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_tiles(const uint32_t *__restrict__ in, uint64_t len, uint32_t *__restrict__ tile_sum) {
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+  uint32_t v = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const uint64_t i = base + (uint64_t)k * kScanThreads + threadIdx.x;
+    if (i < len) v += in[i];
+  }
+  uint32_t total;
+  block_excl_scan(v, &total);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// exclusive scan of the tile sums in place, total at [ntiles]
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(uint32_t *tile_sum, uint32_t ntiles) {
+  const uint32_t per = (ntiles + kScanThreads - 1) / kScanThreads;
+  const uint32_t lo = threadIdx.x * per, hi = lo + per < ntiles ? lo + per : ntiles;
+  uint32_t v = 0;
+  for (uint32_t k = lo; k < hi; ++k) v += tile_sum[k];
+  uint32_t total;
+  uint32_t run = block_excl_scan(v, &total);
+  for (uint32_t k = lo; k < hi; ++k) {
+    const uint32_t t = tile_sum[k];
+    tile_sum[k] = run;
+    run += t;
+  }
+  if (threadIdx.x == 0) tile_sum[ntiles] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_down(const uint32_t *__restrict__ in, uint64_t len, const uint32_t *__restrict__ tile_off,
+                uint32_t ntiles, uint32_t *__restrict__ out, uint32_t *__restrict__ cursor) {
+  const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = base + k < len ? in[base + k] : 0;
+    sum += v[k];
+  }
+  uint32_t total;
+  uint32_t run = tile_off[blockIdx.x] + block_excl_scan(sum, &total);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < len) {
+      out[base + k] = run;
+      if (cursor) cursor[base + k] = run;
+    }
+    run += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[len] = tile_off[ntiles];
+}
+
+int scan_u32(const uint32_t *in, uint64_t len, uint32_t *out, uint32_t *cursor, uint32_t *tiles,
+             cudaStream_t s) {
+  const uint32_t ntiles = (uint32_t)((len + kScanTile - 1) / kScanTile);
+  k_scan_tiles<<<ntiles, kScanThreads, 0, s>>>(in, len, tiles);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_scan_top<<<1, kScanThreads, 0, s>>>(tiles, ntiles);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_scan_down<<<ntiles, kScanThreads, 0, s>>>(in, len, tiles, ntiles, out, cursor);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+__global__ void k_msm_scatter(const uint32_t *__restrict__ digits, uint64_t n, MsmPlan p,
+                              uint32_t *__restrict__ cursor, uint32_t *__restrict__ list) {
+  const uint64_t total = (uint64_t)p.W * n;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t e = digits[t];
+    if (e == kNone) continue;
+    const uint64_t w = t / n, i = t - w * n;
+    const uint32_t pos = warp_increment(cursor, (uint32_t)(w * p.B) + (e >> 1));
+    list[pos] = (uint32_t)i | ((e & 1u) << 31);
+  }
+}
+
+constexpr int kPointThreads = 128;
+constexpr uint32_t kGroup = 32;  // values summed by one thread
+
+// Per bucket at one level: m values to sum.  groups = ceil(m / K) threads; a
+// bucket with m <= K is finished by its one group, otherwise its groups leave
+// ceil(m / K) partial sums for the next level (next = that count, else 0).
+__global__ void k_msm_groups(const uint32_t *__restrict__ m, uint64_t nb,
+                             uint32_t *__restrict__ groups, uint32_t *__restrict__ next) {
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+       b += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = m[b];
+    const uint32_t g = (v + kGroup - 1) / kGroup;
+    groups[b] = g;
+    next[b] = v > kGroup ? g : 0;
+  }
+}
+
+// the bucket whose group range [goff[b], goff[b+1]) holds group t
+__device__ __forceinline__ uint32_t bucket_of(const uint32_t *goff, uint32_t nb, uint32_t t) {
+  uint32_t lo = 0, hi = nb;  // goff[lo] <= t < goff[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (goff[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// One level of bucket sums.  Level 0 (list != null) adds signed affine points
+// named by the sorted list; later levels add XYZZ partial sums.  Group t of
+// bucket b sums values [off[b] + j K, ...) of that bucket (j = t - goff[b]);
+// a finished bucket is written to buckets[b], else to part_out[noff[b] + j].
+__global__ void __launch_bounds__(kPointThreads, 3)
+    k_msm_level(const g1a *__restrict__ points, const uint32_t *__restrict__ list,
+                const g1x *__restrict__ part_in, const uint32_t *__restrict__ m,
+                const uint32_t *__restrict__ off, const uint32_t *__restrict__ goff,
+                const uint32_t *__restrict__ noff, uint32_t nb, g1x *__restrict__ part_out,
+                g1x *__restrict__ buckets) {
+  const uint32_t total = goff[nb];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const uint32_t b = bucket_of(goff, nb, t);
+    const uint32_t j = t - goff[b];
+    const uint32_t cnt = m[b];
+    const uint32_t lo = off[b] + j * kGroup;
+    const uint32_t hi = lo + kGroup < off[b] + cnt ? lo + kGroup : off[b] + cnt;
+    g1x acc = g1x_inf();
+    if (list) {
+      for (uint32_t k = lo; k < hi; ++k) {
+        const uint32_t e = list[k];
+        g1a pt = ld_g1a(points + (e & 0x7fffffffu));
+        if (e >> 31) pt = g1a_neg(pt);
+        acc = g1x_add_affine(acc, pt);
+      }
+    } else {
+      for (uint32_t k = lo; k < hi; ++k) acc = g1x_add(acc, part_in[k]);
+    }
+    if (cnt <= kGroup) buckets[b] = acc;
+    else part_out[noff[b] + j] = acc;
+  }
+}
+
+// Segment s of window w holds buckets b = s G + j, j < G.  Its thread leaves
+// R_s = sum_j B_b and T_s = sum_j (j + 1) B_b (running sums from the top), so
+// that the window sum sum_b (b + 1) B_b = sum_s T_s + G sum_s s R_s.
+__global__ void __launch_bounds__(kPointThreads)
+    k_msm_segments(const g1x *__restrict__ buckets, MsmPlan p, g1x *__restrict__ seg_t,
+                   g1x *__restrict__ seg_r) {
+  const uint64_t total = (uint64_t)p.W * p.S;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const g1x *row = buckets + t * p.G;  // segments are consecutive in each window
+    g1x run = g1x_inf(), sum = g1x_inf();
+    for (int j = (int)p.G - 1; j >= 0; --j) {
+      run = g1x_add(run, row[j]);
+      sum = g1x_add(sum, run);
+    }
+    seg_t[t] = sum;
+    seg_r[t] = run;
+  }
+}
+
+// One block per window: sum_s T_s + G sum_s s R_s.  Thread k takes segments
+// [k m, (k + 1) m) and forms A = sum T_s, V = sum R_s and U = sum (s - k m) R_s;
+// a tree then merges neighbouring ranges with U = U_left + U_right +
+// len_left V_right, where len_left is a power of two (doublings).
+constexpr int kWindowThreads = 64;
+
+__global__ void __launch_bounds__(kWindowThreads)
+    k_msm_windows(const g1x *__restrict__ seg_t, const g1x *__restrict__ seg_r, MsmPlan p,
+                  g1x *__restrict__ win) {
+  extern __shared__ g1x red[];  // A, U, V per thread
+  g1x *sa = red, *su = red + kWindowThreads, *sv = red + 2 * kWindowThreads;
+  const uint32_t w = blockIdx.x, k = threadIdx.x;
+  const uint32_t nthr = p.S < (uint32_t)kWindowThreads ? p.S : (uint32_t)kWindowThreads;
+  const uint32_t m = p.S / nthr;  // both powers of two
+  g1x A = g1x_inf(), U = g1x_inf(), V = g1x_inf();
+  if (k < nthr) {
+    const g1x *t = seg_t + (uint64_t)w * p.S + (uint64_t)k * m;
+    const g1x *r = seg_r + (uint64_t)w * p.S + (uint64_t)k * m;
+    for (int i = (int)m - 1; i >= 0; --i) {
+      A = g1x_add(A, t[i]);
+      if (i > 0) {
+        V = g1x_add(V, r[i]);
+        U = g1x_add(U, V);  // adds R_i once for each of its i index steps
+      }
+    }
+    V = g1x_add(V, r[0]);
+  }
+  sa[k] = A;
+  su[k] = U;
+  sv[k] = V;
+  __syncthreads();
+  uint32_t log_len = 0;  // log2 of the segments a tree node covers
+  for (uint32_t x = m; x > 1; x >>= 1) ++log_len;
+  for (uint32_t h = 1; h < nthr; h <<= 1, ++log_len) {
+    if (k < nthr && (k & (2 * h - 1)) == 0) {
+      sa[k] = g1x_add(sa[k], sa[k + h]);
+      su[k] = g1x_add(g1x_add(su[k], su[k + h]), g1x_dbl_n(sv[k + h], log_len));
+      sv[k] = g1x_add(sv[k], sv[k + h]);
+    }
+    __syncthreads();
+  }
+  if (k == 0) {
+    uint32_t log_g = 0;
+    for (uint32_t x = p.G; x > 1; x >>= 1) ++log_g;
+    win[w] = g1x_add(sa[0], g1x_dbl_n(su[0], log_g));
+  }
+}
+
+// ---- final Horner chain in one warp.  Every lane holds the same point; the
+// independent multiplies of a doubling (3 dependent levels instead of 9
+// multiplies) or of an addition (4 levels instead of 14) run on different
+// lanes and are exchanged by shuffles.
+__device__ __forceinline__ fq shfl_fq(const fq &a, int src) {
+  fq r;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) r.v[i] = __shfl_sync(0xffffffffu, a.v[i], src);
+  return r;
+}
+
+__device__ g1x dbl_warp(const g1x &p) {
+  if (g1x_is_inf(p) || fq_is_zero(p.y)) return g1x_inf();
+  const int lane = threadIdx.x & 31;
+  const fq u = fq_dbl(p.y);
+  // v = u^2 (lane 0), x2 = x^2 (lane 1)
+  fq a = lane == 0 ? u : p.x;
+  fq r = fq_mul(a, a);
+  const fq v = shfl_fq(r, 0), x2 = shfl_fq(r, 1);
+  const fq m = fq_add(fq_dbl(x2), x2);
+  // w = u v (0), s = x v (1), m^2 (2), zz' = v zz (3)
+  a = lane == 0 ? u : lane == 1 ? p.x : lane == 2 ? m : v;
+  fq b = lane == 0 ? v : lane == 1 ? v : lane == 2 ? m : p.zz;
+  r = fq_mul(a, b);
+  const fq w = shfl_fq(r, 0), s = shfl_fq(r, 1), m2 = shfl_fq(r, 2), zz = shfl_fq(r, 3);
+  g1x o;
+  o.x = fq_sub(m2, fq_dbl(s));
+  // zzz' = w zzz (0), m (s - x') (1), w y (2)
+  a = lane == 1 ? m : w;
+  b = lane == 0 ? p.zzz : lane == 1 ? fq_sub(s, o.x) : p.y;
+  r = fq_mul(a, b);
+  o.zzz = shfl_fq(r, 0);
+  o.y = fq_sub(shfl_fq(r, 1), shfl_fq(r, 2));
+  o.zz = zz;
+  return o;
+}
+
+__device__ g1x add_warp(const g1x &p, const g1x &q) {
+  if (g1x_is_inf(q)) return p;
+  if (g1x_is_inf(p)) return q;
+  const int lane = threadIdx.x & 31;
+  // u1 = X1 ZZ2, u2 = X2 ZZ1, s1 = Y1 ZZZ2, s2 = Y2 ZZZ1, ZZ1 ZZ2, ZZZ1 ZZZ2
+  fq a = lane == 0 ? p.x : lane == 1 ? q.x : lane == 2 ? p.y : lane == 3 ? q.y
+         : lane == 4 ? p.zz : p.zzz;
+  fq b = lane == 0 ? q.zz : lane == 1 ? p.zz : lane == 2 ? q.zzz : lane == 3 ? p.zzz
+         : lane == 4 ? q.zz : q.zzz;
+  fq r = fq_mul(a, b);
+  const fq u1 = shfl_fq(r, 0), u2 = shfl_fq(r, 1), s1 = shfl_fq(r, 2), s2 = shfl_fq(r, 3);
+  const fq zz12 = shfl_fq(r, 4), zzz12 = shfl_fq(r, 5);
+  const fq P = fq_sub(u2, u1), R = fq_sub(s2, s1);
+  if (fq_is_zero(P)) return fq_is_zero(R) ? dbl_warp(p) : g1x_inf();
+  // P^2 (0), R^2 (1)
+  a = lane == 0 ? P : R;
+  r = fq_mul(a, a);
+  const fq pp = shfl_fq(r, 0), rr = shfl_fq(r, 1);
+  // P pp (0), u1 pp (1), zz12 pp (2)
+  a = lane == 0 ? P : lane == 1 ? u1 : zz12;
+  r = fq_mul(a, pp);
+  const fq ppp = shfl_fq(r, 0), Q = shfl_fq(r, 1);
+  g1x o;
+  o.zz = shfl_fq(r, 2);
+  o.x = fq_sub(fq_sub(rr, ppp), fq_dbl(Q));
+  // R (Q - x') (0), s1 ppp (1), zzz12 ppp (2)
+  a = lane == 0 ? R : lane == 1 ? s1 : zzz12;
+  b = lane == 0 ? fq_sub(Q, o.x) : ppp;
+  r = fq_mul(a, b);
+  o.y = fq_sub(shfl_fq(r, 0), shfl_fq(r, 1));
+  o.zzz = shfl_fq(r, 2);
+  return o;
+}
+
+// Horner over the windows (one warp), then affine; out = Jacobian (x, y, 1),
+// or all zero for the point at infinity
+__global__ void __launch_bounds__(32) k_msm_final(const g1x *__restrict__ win, MsmPlan p,
+                                                  fq *__restrict__ out) {
+  g1x acc = win[p.W - 1];
+  for (int w = (int)p.W - 2; w >= 0; --w) {
+    for (uint32_t k = 0; k < p.c; ++k) acc = dbl_warp(acc);
+    acc = add_warp(acc, win[w]);
+  }
+  if (threadIdx.x != 0) return;
+  const g1a a = g1x_to_affine(acc);
+  const bool inf = g1x_is_inf(acc);
+  out[0] = a.x;
+  out[1] = a.y;
+  out[2] = inf ? fq_zero() : fq_one();
+}
+
+struct MsmLayout {
+  size_t digits, counts, offsets, cursor, list, groups, goff, next[2], noff[2], part[2], buckets,
+      seg_t, seg_r, win, tiles, total;
+  uint64_t part_cap;  // partial sums one level can leave
+  uint32_t levels;    // group levels: K^levels >= n
+};
+
+MsmLayout msm_layout(uint64_t n, const MsmPlan &p) {
+  MsmLayout L{};
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const uint64_t nb = (uint64_t)p.W * p.B;
+  const uint64_t entries = (uint64_t)p.W * n;
+  // a bucket of m > K values leaves ceil(m / K) <= 2 m / K partial sums
+  L.part_cap = 2 * entries / kGroup + 1;
+  L.levels = 1;
+  for (uint64_t span = kGroup; span < n; span *= kGroup) ++L.levels;
+  size_t o = 0;
+  L.digits = o, o += up(entries * 4);
+  L.counts = o, o += up(nb * 4);
+  L.offsets = o, o += up((nb + 1) * 4);
+  L.cursor = o, o += up(nb * 4);
+  L.list = o, o += up(entries * 4);
+  L.groups = o, o += up(nb * 4);
+  L.goff = o, o += up((nb + 1) * 4);
+  for (int k = 0; k < 2; ++k) {
+    L.next[k] = o, o += up(nb * 4);
+    L.noff[k] = o, o += up((nb + 1) * 4);
+  }
+  L.part[0] = o, o += up(L.part_cap * sizeof(g1x));
+  L.part[1] = o, o += up(L.part_cap * sizeof(g1x));
+  L.buckets = o, o += up(nb * sizeof(g1x));
+  L.seg_t = o, o += up((size_t)p.W * p.S * sizeof(g1x));
+  L.seg_r = o, o += up((size_t)p.W * p.S * sizeof(g1x));
+  L.win = o, o += up((size_t)p.W * sizeof(g1x));
+  L.tiles = o, o += up(((nb + kScanTile - 1) / kScanTile + 1) * 4);
+  L.total = o;
+  return L;
+}
+
+unsigned grid_for(uint64_t work, int threads, int per_sm) {
+  const uint64_t want = (work + threads - 1) / threads;
+  const uint64_t cap = (uint64_t)device_sm_count() * per_sm;
+  return (unsigned)(want < cap ? (want ? want : 1) : cap);
+}
+
+}  // namespace
+}  // namespace pp
+
+extern "C" int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n, void *d_out,
+                         void *stream) {
+  using namespace pp;
+  auto aligned16 = [](const void *q) { return q && (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+  if (!aligned16(d_out) || (n && (!aligned16(d_points) || !aligned16(d_scalars)))) {
+    set_error("pp_msm_g1: buffers must be 16-byte aligned device pointers");
+    return PP_E_INVAL;
+  }
+  if (n >= (1ull << 31)) {
+    set_error("pp_msm_g1: n = %llu points; at most 2^31 - 1", (unsigned long long)n);
+    return PP_E_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n == 0) {
+    PP_CUDA_TRY(cudaMemsetAsync(d_out, 0, 3 * sizeof(fq), s));
+    return PP_OK;
+  }
+  const MsmPlan p = msm_plan(n);
+  if ((uint64_t)p.W * n >= (1ull << 32)) {
+    set_error("pp_msm_g1: n = %llu points is too many for 32-bit bucket offsets",
+              (unsigned long long)n);
+    return PP_E_UNSUPPORTED;
+  }
+  const MsmLayout L = msm_layout(n, p);
+  int st = PP_OK;
+  char *ws = static_cast<char *>(workspace_get(L.total, s, 3, &st));
+  if (st) return st;
+  auto u32 = [&](size_t off) { return reinterpret_cast<uint32_t *>(ws + off); };
+  auto pts = [&](size_t off) { return reinterpret_cast<g1x *>(ws + off); };
+  uint32_t *digits = u32(L.digits), *counts = u32(L.counts), *offsets = u32(L.offsets);
+  uint32_t *cursor = u32(L.cursor), *list = u32(L.list), *groups = u32(L.groups);
+  uint32_t *goff = u32(L.goff), *tiles = u32(L.tiles);
+  g1x *buckets = pts(L.buckets), *seg_t = pts(L.seg_t), *seg_r = pts(L.seg_r), *win = pts(L.win);
+  const uint64_t nb = (uint64_t)p.W * p.B;
+
+  // 1-3: signed digits, bucket sizes, counting sort of (point, sign) by bucket
+  PP_CUDA_TRY(cudaMemsetAsync(counts, 0, nb * 4, s));
+  k_msm_digits<<<grid_for(n, 256, 8), 256, 0, s>>>(static_cast<const uint32_t *>(d_scalars), n, p,
+                                                    digits, counts);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  if ((st = scan_u32(counts, nb, offsets, cursor, tiles, s))) return st;
+  k_msm_scatter<<<grid_for((uint64_t)p.W * n, 256, 8), 256, 0, s>>>(digits, n, p, cursor, list);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+
+  // 4: bucket sums, at most K values per thread, over L.levels levels
+  PP_CUDA_TRY(cudaMemsetAsync(buckets, 0, nb * sizeof(g1x), s));  // all zero = infinity
+  const uint32_t *m = counts, *off = offsets;
+  const g1x *part_in = nullptr;
+  for (uint32_t lv = 0; lv < L.levels; ++lv) {
+    uint32_t *next = u32(L.next[lv & 1]), *noff = u32(L.noff[lv & 1]);
+    g1x *part_out = pts(L.part[lv & 1]);
+    k_msm_groups<<<grid_for(nb, 256, 8), 256, 0, s>>>(m, nb, groups, next);
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    if ((st = scan_u32(groups, nb, goff, nullptr, tiles, s))) return st;
+    if ((st = scan_u32(next, nb, noff, nullptr, tiles, s))) return st;
+    k_msm_level<<<grid_for((uint64_t)p.W * n / 4 + nb, kPointThreads, 16), kPointThreads, 0, s>>>(
+        static_cast<const g1a *>(d_points), lv == 0 ? list : nullptr, part_in, m, off, goff, noff,
+        (uint32_t)nb, part_out, buckets);
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    m = next;
+    off = noff;
+    part_in = part_out;
+  }
+
+  // 5-7: weighted bucket sums per window, windows combined, affine result
+  k_msm_segments<<<grid_for((uint64_t)p.W * p.S, kPointThreads, 16), kPointThreads, 0, s>>>(
+      buckets, p, seg_t, seg_r);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_windows<<<p.W, kWindowThreads, 3 * kWindowThreads * sizeof(g1x), s>>>(seg_t, seg_r, p,
+                                                                                 win);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_final<<<1, 32, 0, s>>>(win, p, static_cast<fq *>(d_out));
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
+}
+
+extern "C" int pp_msm_g1_window_bits(uint64_t n) { return (int)pp::msm_plan(n).c; }

@@ -18,6 +18,8 @@
 //       inputs <dir>/<argument name>.bin -> <dir>/quotient_out.bin
 //   pp_compat_driver gate <n> <sbox_alpha> <dir>
 //       compute_gate_constraint_allmerge_cuda -> <dir>/gate_out.bin
+//   pp_compat_driver msm <n> <points.bin> <scalars.bin> <out.bin>
+//       multi_scalar_mult -> out.bin (Jacobian x, y, 1)
 //   pp_compat_driver convert <n> <in.bin> <outdir>
 //       read_file, to_base -> base.bin and base.txt (writeToFile), to_mont of
 //       that -> mont.bin (the input again)
@@ -158,6 +160,17 @@ static int gate(size_t n, long long alpha, const std::string &dir) {
   return 0;
 }
 
+static int msm(size_t n, const std::string &pts, const std::string &scs, const std::string &out) {
+  SyncedMemory p(n * 96), s(n * 32);
+  auto pv = read_file(pts, n * 96), sv = read_file(scs, n * 32);
+  std::memcpy(p.mutable_cpu_data(), pv.data(), n * 96);
+  std::memcpy(s.mutable_cpu_data(), sv.data(), n * 32);
+  SyncedMemory r = multi_scalar_mult(p, s);
+  write_file(out, r.mutable_cpu_data(), 144);
+  std::printf("msm ok\n");
+  return 0;
+}
+
 static int convert(size_t n, const std::string &in, const std::string &outdir) {
   SyncedMemory x(n * 32);
   ::read_file(in.c_str(), x.mutable_cpu_data());
@@ -177,6 +190,8 @@ int main(int argc, char **argv) {
     if (argc >= 5 && std::string(argv[1]) == "ntt") return ntt_check(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 4 && std::string(argv[1]) == "quotient")
       return quotient(std::strtoull(argv[2], nullptr, 10), argv[3]);
+    if (argc >= 6 && std::string(argv[1]) == "msm")
+      return msm(std::strtoull(argv[2], nullptr, 10), argv[3], argv[4], argv[5]);
     if (argc >= 5 && std::string(argv[1]) == "convert")
       return convert(std::strtoull(argv[2], nullptr, 10), argv[3], argv[4]);
     if (argc >= 5 && std::string(argv[1]) == "gate")
@@ -188,6 +203,6 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
     return 3;
   }
-  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate|convert ...\n", argv[0]);
+  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate|convert|msm ...\n", argv[0]);
   return 1;
 }

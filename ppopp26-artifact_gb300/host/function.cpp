@@ -238,3 +238,17 @@ float naive_lde(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, int, int, int
 }
 
 SyncedMemory last_lde_output() { return g_last_lde; }
+
+// ------------------------------------------------------------------- MSM ---
+SyncedMemory multi_scalar_mult(SyncedMemory points, SyncedMemory scalars, cudaStream_t stream) {
+  if (points.size() % 96 || scalars.size() % 32)
+    throw pp::Error(PP_E_INVAL, "multi_scalar_mult: sizes are not whole points / scalars");
+  const uint64_t np = points.size() / 96, ns = scalars.size() / 32;
+  const uint64_t n = np < ns ? np : ns;
+  SyncedMemory out(3 * 48);
+  void *o = out.mutable_gpu_data_async(stream);
+  const void *p = n ? points.mutable_gpu_data_async(stream) : nullptr;
+  const void *s = n ? scalars.mutable_gpu_data_async(stream) : nullptr;
+  pp::check(pp_msm_g1(p, s, n, o, stream), "multi_scalar_mult");
+  return out;
+}

@@ -80,3 +80,10 @@ float our_lde(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, int lg_k, int s
 float naive_lde(cpu::BLS12_381_Fr_G1 *input, int lg_N, int lambda, int lg_k, int pad_threads,
                 int transpose_threads, Ntt &ntt);
 SyncedMemory last_lde_output();
+
+// PLONK/utils/function.cuh:144: sum_i scalars[i] * points[i] over G1.  points
+// holds affine (x, y) Fq pairs (96 bytes each, Montgomery form), scalars plain
+// 256-bit integers (32 bytes each); the first min(#points, #scalars) pairs are
+// used.  Returns a 144-byte Jacobian point (x, y, 1), all zero for infinity.
+SyncedMemory multi_scalar_mult(SyncedMemory points, SyncedMemory scalars,
+                               cudaStream_t stream = (cudaStream_t)0);

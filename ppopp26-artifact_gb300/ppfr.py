@@ -43,6 +43,8 @@ def lib():
                 "pp_lde": [v, v, u32, u32, u32, v],
                 "pp_ntt_host": [v, v, u32, i, v],
                 "pp_to_mont": [v, v, u64, v],
+                "pp_msm_g1": [v, v, u64, v, v],
+                "pp_msm_g1_window_bits": [u64],
                 "pp_to_base": [v, v, u64, v],
                 "pp_count_noncanonical": [v, u64, v, v],
                 "pp_lde_host": [v, v, u32, u32, u32, v],
@@ -164,6 +166,26 @@ def lde_host(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):
         out = empty_pinned(x.shape[0] << lam)
     check(lib().pp_lde_host(_hptr(x), _hptr(out), lg, lam, mode, _stream(stream)))
     return out
+
+
+# ------------------------------------------------------------------------ G1
+def msm_g1(points, scalars, out=None, stream=None):
+    """pp_msm_g1: points (n, 12) int64 (affine x, y over Fq, Montgomery),
+    scalars (n, 4) int64 (plain integers) -> (3, 6) int64 Jacobian point
+    (x, y, 1), all zero for infinity."""
+    torch = _torch()
+    n = points.shape[0]
+    assert scalars.shape[0] == n and points.shape[1] == 12 and scalars.shape[1] == 4
+    assert points.is_contiguous() and scalars.is_contiguous()
+    if out is None:
+        out = torch.empty((3, 6), dtype=torch.int64, device=points.device)
+    pp_, sp_ = (ctypes.c_void_p(points.data_ptr()), ctypes.c_void_p(scalars.data_ptr())) if n else (None, None)
+    check(lib().pp_msm_g1(pp_, sp_, n, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+    return out
+
+
+def msm_window_bits(n: int) -> int:
+    return int(lib().pp_msm_g1_window_bits(n))
 
 
 # -------------------------------------------------------------- data formats

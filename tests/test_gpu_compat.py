@@ -98,3 +98,15 @@ def test_gate_driver_matches_golden(pp, cuda, tmp_path, case):
     n = g[t + "out"].shape[0]
     run("gate", n, int(g[t + "SBOX_ALPHA"][0]), tmp_path)
     assert np.array_equal(load(tmp_path / "gate_out.bin", n), g[t + "out"])
+
+
+@pytest.mark.parametrize("case", ["rand_n64", "edge_n16"])
+def test_msm_driver_matches_blst(pp, cuda, tmp_path, case):
+    """multi_scalar_mult through the C++ layer (PLONK/utils/function.cuh:144)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "msm.npz"))
+    pts, sc = g[case + "/points"], g[case + "/scalars"]
+    pts.tofile(tmp_path / "p.bin")
+    sc.tofile(tmp_path / "s.bin")
+    run("msm", len(pts), tmp_path / "p.bin", tmp_path / "s.bin", tmp_path / "o.bin")
+    o = np.fromfile(tmp_path / "o.bin", dtype=np.uint64).reshape(3, 6)
+    assert np.array_equal(np.concatenate([o[0], o[1]]), g[case + "/out"])
