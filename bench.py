@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--lean", action="store_true",
                     help="device timing only (no e2e, CPU baseline, ops): the profiling case")
     ap.add_argument("--lg", type=int, default=LG_N, help="transform size (profiling of smaller cases)")
+    ap.add_argument("--op", default="ntt", choices=["ntt", "msm", "gate", "perm"],
+                    help="with --lean: time one operator alone at 2^lg points (profiling case)")
     return ap.parse_args()
 
 
@@ -206,6 +208,13 @@ def run_ours(args, rank, world, local):
     def barrier():
         if dist:
             dist.barrier()
+
+    if args.lean and args.op != "ntt":
+        if rank == 0:
+            profile_op(args, pp, torch)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     # ---- device-resident headline
     n = 1 << args.lg
@@ -443,6 +452,41 @@ def constraint_bench(pp, torch, rate, res):
     for k, mm in (("quotient_permutation_2^22", 18), ("gate_constraint_2^22", 104)):
         pts = res[k]["Melem_per_s"] * 1e6
         res[k]["int_frac_of_nominal_peak"] = round(pts * mm * 256 / peak, 4)
+
+
+def profile_op(args, pp, torch):
+    """--lean --op msm|gate|perm: one operator at 2^lg points, device time
+    only (the profiling case for ncu launch lists of those kernels)."""
+    import numpy as np
+
+    ppfr = pp.ppfr
+    n = 1 << args.lg
+    if args.op == "msm":
+        from oracle import oracle as O
+
+        base = O.g1_mul_gen(O.random_fr(1024, 77))
+        reps = max(1, n // 1024)
+        pts = torch.from_numpy(np.ascontiguousarray(np.tile(base, (reps, 1))[:n]).view(np.int64)).cuda()
+        sc = ppfr.random_fr(n, 5)
+        out = torch.empty((3, 6), dtype=torch.int64, device="cuda")
+        fn = lambda: ppfr.msm_g1(pts, sc, out=out)  # noqa: E731
+    elif args.op == "gate":
+        V = {k: ppfr.random_fr(n, 0x20 + i) for i, k in enumerate(ppfr.GATE_VECTORS)}
+        S = {k: ppfr.random_fr(1, 0x80 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
+        out = ppfr.empty(n)
+        fn = lambda: ppfr.gate_constraint(V, S, 5, out=out)  # noqa: E731
+    else:
+        vec = [ppfr.random_fr(n, 0xC0 + i) for i in range(13)]
+        sca = [ppfr.random_fr(1, 0xD0 + i) for i in range(7)]
+        out = ppfr.empty(n)
+        fn = lambda: ppfr.quotient_permutation(  # noqa: E731
+            vec[8], vec[0:4], vec[9], vec[10], vec[4:8], vec[11], vec[12], sca[3], sca[4], sca[5],
+            sca[0:3], sca[6], out=out)
+    l0 = pp.launch_count()
+    ms = time_device(fn, args.steps, args.warmup, torch)
+    print(json.dumps({"metric": "%s_2^%d" % (args.op, args.lg), "lean": True,
+                      "ms_per_step": round(ms / args.steps, 4),
+                      "gpu_launches": int(pp.launch_count() - l0)}), flush=True)
 
 
 def msm_bench(pp, torch, rate, res):
