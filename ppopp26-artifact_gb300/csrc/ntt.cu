@@ -246,12 +246,33 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
         const uint32_t c = d & ((1u << lgSj) - 1), prefix = d >> lgSj;
         const uint32_t pb = (prefix << (lgSj + 3)) + c;
         fr x[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) x[i] = tile.get(pb + ((uint32_t)i << lgSj), col);
         const fr w1 = ldg_fr(a.tw_inner + (R >> 3));
         const fr w2 = ldg_fr(a.tw_inner + (R >> 2));
         const fr w3 = ldg_fr(a.tw_inner + 3 * (R >> 3));
-        dft8(x, w1, w2, w3);
+        if (lgP == 0 && a.zero_lg >= 3) {
+          // first round over zero padding: only x[0] can be non-zero, and the
+          // 8-point DFT of (x0, 0, ..., 0) is x0 in every output
+          x[0] = tile.get(pb, col);
+#pragma unroll
+          for (int i = 1; i < 8; ++i) x[i] = x[0];
+        } else if (lgP == 0 && a.zero_lg == 2) {
+          // only x[0], x[1] can be non-zero: X[k] = x0 + x1 w^k, w^4 = -1,
+          // stored bit-reversed like dft8 (x[i] = X[bitrev3(i)])
+          const fr x0 = tile.get(pb, col), x1 = tile.get(pb + (1u << lgSj), col);
+          const fr t1 = fr_mul(x1, w1), t2 = fr_mul(x1, w2), t3 = fr_mul(x1, w3);
+          x[0] = fr_add(x0, x1);
+          x[1] = fr_sub(x0, x1);
+          x[2] = fr_add(x0, t2);
+          x[3] = fr_sub(x0, t2);
+          x[4] = fr_add(x0, t1);
+          x[5] = fr_sub(x0, t1);
+          x[6] = fr_add(x0, t3);
+          x[7] = fr_sub(x0, t3);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = tile.get(pb + ((uint32_t)i << lgSj), col);
+          dft8(x, w1, w2, w3);
+        }
         // x[i] holds output k = bitrev3(i)
         if (lgSj > 0) {
 #pragma unroll
@@ -708,6 +729,14 @@ int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool invers
     a.first = j == 0;
     a.last = j + 1 == plan->P;
     a.unit_in = a.first && in.in_host;
+    // zero-padded input (n_valid = N / 2^z): pass 1's rows >= R >> z are zero
+    a.zero_lg = 0;
+    if (a.first && !a.last && in.kind != NTT_IN_SPREAD && in.n_valid && in.n_valid < N &&
+        (in.n_valid & (in.n_valid - 1)) == 0) {
+      uint32_t z = 0;
+      while ((in.n_valid << z) < N) ++z;
+      a.zero_lg = z;
+    }
     a.unit_out = a.last && in.out_host;
     a.in = j == 0 ? d_in : work;
     a.out = a.last ? d_out : work;

@@ -21,6 +21,7 @@ struct PassArgs {
   uint32_t lgR, lgT, lgS, lgN;
   uint32_t first, last, has_post_scale, in_kind, spread;
   uint32_t unit_in, unit_out;  // move 16-byte halves (host-memory input / output)
+  uint32_t zero_lg;  // first pass: rows >= R >> zero_lg of every tile are zero (padding)
   uint32_t P;
   uint32_t lgRp[4];
 };
