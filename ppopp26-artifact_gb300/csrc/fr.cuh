@@ -712,6 +712,10 @@ PP_HD void row9_red(uint32_t t[10]) {
   t[9] = 0;
 }
 
+// LAZY: skip the final subtraction.  For b < r and any 256-bit a the result
+// is < 2r: every row keeps t < b + r, and at the end
+// t = (a b + m r) / R < (R r + R r) / R = 2r.
+template <bool LAZY = false>
 PP_HD fr fr_mul_row9(const fr &a, const fr &b) {
   uint32_t t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
@@ -719,7 +723,7 @@ PP_HD fr fr_mul_row9(const fr &a, const fr &b) {
     row9_ab(t, a.v[i], b.v);
     row9_red(t);
   }
-  fr_reduce_once(t);
+  if (!LAZY) fr_reduce_once(t);
   fr out;
 #pragma unroll
   for (int i = 0; i < 8; ++i) out.v[i] = t[i];
@@ -910,6 +914,78 @@ PP_HD fr fr_mul(const fr &a, const fr &b) {
 }
 
 PP_HD fr fr_sqr(const fr &a) { return fr_mul(a, a); }
+
+// ---- lazy arithmetic on [0, 2r) for the NTT's inner rounds: values stay
+// below 2r and are made canonical once, when the transform stores its
+// result.  fr_mul_lazy takes a < 2r and b < r (the twiddle) and returns a
+// value < 2r.
+PP_HD fr fr_mul_lazy(const fr &a, const fr &b) {
+#if PP_MUL_VARIANT == 9
+  return fr_mul_row9<true>(a, b);
+#else
+  fr c = a;
+  fr_reduce_once(c.v);
+  return fr_mul(c, b);
+#endif
+}
+
+// 2r, least significant limb first
+#define PP_2R0 0x00000002u
+#define PP_2R1 0xfffffffeu
+#define PP_2R2 0xfffcb7fdu
+#define PP_2R3 0xa77b4805u
+#define PP_2R4 0x1343b00au
+#define PP_2R5 0x6673b010u
+#define PP_2R6 0x533afa90u
+#define PP_2R7 0xe7db4ea6u
+
+// a + b mod 2r for a, b < 2r: a + b < 4r may carry out of 256 bits
+PP_HD fr fr_add_lazy(const fr &a, const fr &b) {
+  uint32_t s[8], d[8];
+  s[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) s[i] = addc_cc(a.v[i], b.v[i]);
+  const uint32_t carry = addc(0, 0);
+  d[0] = sub_cc(s[0], PP_2R0);
+  d[1] = subc_cc(s[1], PP_2R1);
+  d[2] = subc_cc(s[2], PP_2R2);
+  d[3] = subc_cc(s[3], PP_2R3);
+  d[4] = subc_cc(s[4], PP_2R4);
+  d[5] = subc_cc(s[5], PP_2R5);
+  d[6] = subc_cc(s[6], PP_2R6);
+  d[7] = subc_cc(s[7], PP_2R7);
+  const uint32_t borrow = subc(0, 0);        // all ones when s < 2r (as 256 bits)
+  const uint32_t keep = borrow & (carry - 1u);  // ... and there was no carry
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = keep ? s[i] : d[i];
+  return r;
+}
+
+// a - b mod 2r for a, b < 2r
+PP_HD fr fr_sub_lazy(const fr &a, const fr &b) {
+  fr d;
+  d.v[0] = sub_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int i = 1; i < 8; ++i) d.v[i] = subc_cc(a.v[i], b.v[i]);
+  const uint32_t mask = subc(0, 0);  // all ones on borrow
+  d.v[0] = add_cc(d.v[0], PP_2R0 & mask);
+  d.v[1] = addc_cc(d.v[1], PP_2R1 & mask);
+  d.v[2] = addc_cc(d.v[2], PP_2R2 & mask);
+  d.v[3] = addc_cc(d.v[3], PP_2R3 & mask);
+  d.v[4] = addc_cc(d.v[4], PP_2R4 & mask);
+  d.v[5] = addc_cc(d.v[5], PP_2R5 & mask);
+  d.v[6] = addc_cc(d.v[6], PP_2R6 & mask);
+  d.v[7] = addc(d.v[7], PP_2R7 & mask);
+  return d;
+}
+
+// canonical form of a value < 2r
+PP_HD fr fr_canon(const fr &a) {
+  fr r = a;
+  fr_reduce_once(r.v);
+  return r;
+}
 
 // a^e for a 64-bit exponent (square and multiply, most significant bit first)
 PP_HD fr fr_pow_u64(const fr &a, uint64_t e) {

@@ -250,7 +250,7 @@ __global__ void k_msm_scatter(const uint32_t *__restrict__ digits, uint64_t n, M
 }
 
 constexpr int kPointThreads = 128;
-constexpr uint32_t kGroup = 32;  // values summed by one thread
+constexpr uint32_t kGroup = 16;  // values summed by one thread (16 beat 32 and 64 on GB300)
 
 // Per bucket at one level: m values to sum.  groups = ceil(m / K) threads; a
 // bucket with m <= K is finished by its one group, otherwise its groups leave

@@ -91,10 +91,12 @@ struct SmemTile {
   }
 };
 
+// Inside a transform values are kept below 2r (fr_*_lazy); the last round of
+// the last pass makes them canonical before they leave the kernel.
 __device__ __forceinline__ void bfly(fr &a, fr &b) {
   const fr t = a;
-  a = fr_add(t, b);
-  b = fr_sub(t, b);
+  a = fr_add_lazy(t, b);
+  b = fr_sub_lazy(t, b);
 }
 
 // 8-point DFT, decimation in frequency; afterwards x[i] = X[bitrev3(i)]
@@ -103,15 +105,15 @@ __device__ __forceinline__ void dft8(fr x[8], const fr &w1, const fr &w2, const 
   bfly(x[1], x[5]);
   bfly(x[2], x[6]);
   bfly(x[3], x[7]);
-  x[5] = fr_mul(x[5], w1);
-  x[6] = fr_mul(x[6], w2);
-  x[7] = fr_mul(x[7], w3);
+  x[5] = fr_mul_lazy(x[5], w1);
+  x[6] = fr_mul_lazy(x[6], w2);
+  x[7] = fr_mul_lazy(x[7], w3);
   bfly(x[0], x[2]);
   bfly(x[1], x[3]);
   bfly(x[4], x[6]);
   bfly(x[5], x[7]);
-  x[3] = fr_mul(x[3], w2);
-  x[7] = fr_mul(x[7], w2);
+  x[3] = fr_mul_lazy(x[3], w2);
+  x[7] = fr_mul_lazy(x[7], w2);
   bfly(x[0], x[1]);
   bfly(x[2], x[3]);
   bfly(x[4], x[5]);
@@ -220,7 +222,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
           v = (g & ((1ull << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (g >> a.spread)) : fr_zero();
         } else if (g < a.n_valid) {
           v = ldcs_fr(a.in + g);
-          if (a.in_kind == NTT_IN_DIAG) v = fr_mul(v, ldcs_fr(a.diag + g));
+          if (a.in_kind == NTT_IN_DIAG) v = fr_mul_lazy(v, ldcs_fr(a.diag + g));
         } else {
           v = fr_zero();
         }
@@ -259,15 +261,15 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
           // only x[0], x[1] can be non-zero: X[k] = x0 + x1 w^k, w^4 = -1,
           // stored bit-reversed like dft8 (x[i] = X[bitrev3(i)])
           const fr x0 = tile.get(pb, col), x1 = tile.get(pb + (1u << lgSj), col);
-          const fr t1 = fr_mul(x1, w1), t2 = fr_mul(x1, w2), t3 = fr_mul(x1, w3);
-          x[0] = fr_add(x0, x1);
-          x[1] = fr_sub(x0, x1);
-          x[2] = fr_add(x0, t2);
-          x[3] = fr_sub(x0, t2);
-          x[4] = fr_add(x0, t1);
-          x[5] = fr_sub(x0, t1);
-          x[6] = fr_add(x0, t3);
-          x[7] = fr_sub(x0, t3);
+          const fr t1 = fr_mul_lazy(x1, w1), t2 = fr_mul_lazy(x1, w2), t3 = fr_mul_lazy(x1, w3);
+          x[0] = fr_add_lazy(x0, x1);
+          x[1] = fr_sub_lazy(x0, x1);
+          x[2] = fr_add_lazy(x0, t2);
+          x[3] = fr_sub_lazy(x0, t2);
+          x[4] = fr_add_lazy(x0, t1);
+          x[5] = fr_sub_lazy(x0, t1);
+          x[6] = fr_add_lazy(x0, t3);
+          x[7] = fr_sub_lazy(x0, t3);
         } else {
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = tile.get(pb + ((uint32_t)i << lgSj), col);
@@ -278,8 +280,11 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
 #pragma unroll
           for (int i = 1; i < 8; ++i) {
             const uint32_t k = ((i & 1) << 2) | (i & 2) | ((i >> 2) & 1);
-            x[i] = fr_mul(x[i], ldg_fr(a.tw_inner + ((c * k) << lgP)));
+            x[i] = fr_mul_lazy(x[i], ldg_fr(a.tw_inner + ((c * k) << lgP)));
           }
+        } else if (a.last) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -297,7 +302,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
           for (int h = 0; h < 8; h += 4) {
             bfly(x[h + 0], x[h + 2]);
             bfly(x[h + 1], x[h + 3]);
-            x[h + 3] = fr_mul(x[h + 3], w4);
+            x[h + 3] = fr_mul_lazy(x[h + 3], w4);
             bfly(x[h + 0], x[h + 1]);
             bfly(x[h + 2], x[h + 3]);
             const fr t = x[h + 1];  // bit-reversed -> natural
@@ -307,6 +312,10 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
         } else {
 #pragma unroll
           for (int h = 0; h < 8; h += 2) bfly(x[h], x[h + 1]);
+        }
+        if (a.last) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) tile.put((d << 3) + i, col, x[i]);
@@ -349,7 +358,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
     }
     fr v = tile.get(digit_reverse(o, a.lgR), col);
     if (!a.last) {
-      if (a.tw_layer) v = fr_mul(v, ldcs_fr(a.tw_layer + ((uint64_t)o << a.lgS) + col0 + col));
+      if (a.tw_layer) v = fr_mul_lazy(v, ldcs_fr(a.tw_layer + ((uint64_t)o << a.lgS) + col0 + col));
       st_fr(a.out + base + ((uint64_t)o << a.lgS) + col, v);
     } else {
       if (a.has_post_scale) v = fr_mul(v, a.post_scale);

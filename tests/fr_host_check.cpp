@@ -19,6 +19,40 @@ static fr load(const uint64_t *p) {
   return a;
 }
 
+static const uint32_t kR[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+
+// a + r for a < r (the other representative of a below 2r)
+static fr plus_r(const fr &a) {
+  fr s;
+  uint64_t c = 0;
+  for (int i = 0; i < 8; ++i) {
+    c += (uint64_t)a.v[i] + kR[i];
+    s.v[i] = (uint32_t)c;
+    c >>= 32;
+  }
+  return s;
+}
+
+static bool below_2r(const fr &a) {
+  // compare a with 2r from the top limb down
+  uint32_t two_r[8];
+  uint64_t c = 0;
+  for (int i = 0; i < 8; ++i) {
+    c += 2ull * kR[i];
+    two_r[i] = (uint32_t)c;
+    c >>= 32;
+  }
+  for (int i = 7; i >= 0; --i)
+    if (a.v[i] != two_r[i]) return a.v[i] < two_r[i];
+  return false;
+}
+
+// the lazy form must stay below 2r and be congruent to the canonical answer
+static bool lazy_ok(const fr &lazy, const uint64_t want[4]) {
+  const fr c = pp::fr_canon(lazy);
+  return below_2r(lazy) && std::memcmp(c.v, want, 32) == 0;
+}
+
 int main(int argc, char **argv) {
   const uint64_t n = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 20000;
   uint64_t *a = new uint64_t[4 * n], *b = new uint64_t[4 * n];
@@ -32,6 +66,11 @@ int main(int argc, char **argv) {
   std::memcpy(a + 8, rm1, 32);
   std::memcpy(b + 8, rm1, 32);
   or_fr_one(a + 12);
+  // r - 1 at odd indices: the lazy operands there reach 2r - 1
+  std::memcpy(a + 20, rm1, 32);
+  std::memcpy(b + 20, rm1, 32);
+  std::memcpy(a + 28, rm1, 32);
+  std::memcpy(b + 28, rm1, 32);
   long bad = 0;
   for (uint64_t i = 0; i < n; ++i) {
     fr x = load(a + 4 * i), y = load(b + 4 * i);
@@ -49,14 +88,20 @@ int main(int argc, char **argv) {
         std::memcmp(m12.v, want, 32) || std::memcmp(m13.v, want, 32)) {
       if (bad++ < 5) std::printf("mul mismatch at %llu\n", (unsigned long long)i);
     }
+    // lazy operands: either representative below 2r
+    const fr xl = (i & 1) ? plus_r(x) : x, yl = (i & 2) ? plus_r(y) : y;
+    const fr ml = pp::fr_mul_lazy(xl, y), mc = pp::fr_mul_row9(xl, y);
+    if (!lazy_ok(ml, want) || std::memcmp(mc.v, want, 32)) {
+      if (bad++ < 5) std::printf("lazy mul mismatch at %llu\n", (unsigned long long)i);
+    }
     or_fr_add(a + 4 * i, b + 4 * i, want);
     fr s = pp::fr_add(x, y);
-    if (std::memcmp(s.v, want, 32)) {
+    if (std::memcmp(s.v, want, 32) || !lazy_ok(pp::fr_add_lazy(xl, yl), want)) {
       if (bad++ < 5) std::printf("add mismatch at %llu\n", (unsigned long long)i);
     }
     or_fr_sub(a + 4 * i, b + 4 * i, want);
     fr d = pp::fr_sub(x, y);
-    if (std::memcmp(d.v, want, 32)) {
+    if (std::memcmp(d.v, want, 32) || !lazy_ok(pp::fr_sub_lazy(xl, yl), want)) {
       if (bad++ < 5) std::printf("sub mismatch at %llu\n", (unsigned long long)i);
     }
     if (i < 200) {
