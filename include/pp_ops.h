@@ -316,8 +316,9 @@ int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n, void *str
  * cuda::msm_zkp_cuda (PLONK/utils/zkp/cuda/zksnark_msm.cu:48-88) and
  * cpu::msm_collect_cpu (PLONK/utils/zkp/cpu/msmcollect.cpp:5-41); the final
  * window aggregation runs on the GPU.  n < 2^31.  Uses a per-stream device
- * workspace of about 56 W n + 230 W 2^(c-1) bytes (c = window bits, W =
- * 256 / c + 1 windows; pp_msm_g1_window_bits gives c). */
+ * workspace of at most 56 W n + 360 W 2^(c-1) bytes (c = window bits, W =
+ * 256 / c + 1 windows; pp_msm_g1_window_bits gives c): 1.1 GB for 2^20
+ * points, 4.0 GB for 2^22. */
 int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n, void *d_out, void *stream);
 int pp_msm_g1_window_bits(uint64_t n);
 

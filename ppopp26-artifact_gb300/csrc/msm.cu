@@ -21,8 +21,10 @@
 //                few-bit top window), so no thread sums more than K values
 //   5. segments  one thread per run of G buckets: running sums T = sum
 //                (j + 1) B and R = sum B over its run
-//   6. windows   one block per window: sum T + G sum s R_s, the index weights
-//                merged up a tree with power-of-two doublings
+//   6. windows   sum T + G sum_s s R_s with sum_s s R_s = sum_k 2^k Q_k, Q_k
+//                the R_s whose index has bit k set: plain sums in chunks, a
+//                block tree per sum, then one warp per window for the Horner
+//                chain over k
 //   7. final     one warp: Horner over the windows (c doublings each, the
 //                independent multiplies of each step on different lanes), one
 //                inversion to affine
@@ -39,12 +41,19 @@ namespace {
 constexpr uint32_t kNone = 0xffffffffu;
 
 struct MsmPlan {
-  uint32_t c;  // window bits
-  uint32_t W;  // windows: W c >= 257, so the top window's carry has a home
-  uint32_t B;  // buckets per window, 2^(c-1)
-  uint32_t G;  // buckets per aggregation segment
-  uint32_t S;  // segments per window, B / G
+  uint32_t c;    // window bits
+  uint32_t W;    // windows: W c >= 257, so the top window's carry has a home
+  uint32_t B;    // buckets per window, 2^(c-1)
+  uint32_t G;    // buckets per aggregation segment
+  uint32_t S;    // segments per window, B / G
+  uint32_t lgG;  // log2 G
+  uint32_t lgS;  // log2 S
 };
+
+// Buckets per segment: the longest run (fewer, cheaper window sums) that still
+// gives 2^15 segment threads.  On GB300 this beat fixed 4, 8 and 16 (2^16
+// points: 16 -> 4.65 ms, 4 -> 3.92 ms; 2^22: 4 -> 53.2 ms, 16 -> 51.3 ms).
+constexpr uint32_t kSegmentMax = 16, kSegmentMin = 4, kSegmentThreads = 1u << 15;
 
 // minimise W (10 n + 14 2^c) Fq multiplies: the bucket sums (one mixed add
 // per point and window) against the aggregation (two adds per bucket)
@@ -61,8 +70,11 @@ MsmPlan msm_plan(uint64_t n) {
   }
   p.W = 256 / p.c + 1;
   p.B = 1u << (p.c - 1);
-  p.G = p.B < 32 ? p.B : 32;
+  p.G = kSegmentMax;  // B >= 32 (c >= 6)
+  while (p.G > kSegmentMin && (uint64_t)p.W * p.B / p.G < kSegmentThreads) p.G >>= 1;
   p.S = p.B / p.G;
+  while ((1u << p.lgG) < p.G) ++p.lgG;
+  while ((1u << p.lgS) < p.S) ++p.lgS;
   return p;
 }
 
@@ -330,52 +342,78 @@ __global__ void __launch_bounds__(kPointThreads)
   }
 }
 
-// One block per window: sum_s T_s + G sum_s s R_s.  Thread k takes segments
-// [k m, (k + 1) m) and forms A = sum T_s, V = sum R_s and U = sum (s - k m) R_s;
-// a tree then merges neighbouring ranges with U = U_left + U_right +
-// len_left V_right, where len_left is a power of two (doublings).
-constexpr int kWindowThreads = 64;
+// Window sums from the segments: sum_b (b + 1) B_b = sum_s T_s + G sum_s s R_s,
+// and sum_s s R_s = sum_k 2^k Q_k, where Q_k adds the R_s of the segments whose
+// index s has bit k set.  So a window needs 1 + lg S plain sums (sum j = 0 is
+// sum_s T_s, sum j = 1 + k is Q_k) and one short Horner chain; no sum weights
+// a point by more than one doubling at a time.
+//
+// Each sum is cut into chunks of kChunk terms; one thread adds one chunk.
+// Window w's chunks are part[w ncw + u]: u < nc0 for sum 0, then nc1 chunks
+// for each Q_k in order of k.
+constexpr uint32_t kChunk = 16;
 
-__global__ void __launch_bounds__(kWindowThreads)
-    k_msm_windows(const g1x *__restrict__ seg_t, const g1x *__restrict__ seg_r, MsmPlan p,
-                  g1x *__restrict__ win) {
-  extern __shared__ g1x red[];  // A, U, V per thread
-  g1x *sa = red, *su = red + kWindowThreads, *sv = red + 2 * kWindowThreads;
-  const uint32_t w = blockIdx.x, k = threadIdx.x;
-  const uint32_t nthr = p.S < (uint32_t)kWindowThreads ? p.S : (uint32_t)kWindowThreads;
-  const uint32_t m = p.S / nthr;  // both powers of two
-  g1x A = g1x_inf(), U = g1x_inf(), V = g1x_inf();
-  if (k < nthr) {
-    const g1x *t = seg_t + (uint64_t)w * p.S + (uint64_t)k * m;
-    const g1x *r = seg_r + (uint64_t)w * p.S + (uint64_t)k * m;
-    for (int i = (int)m - 1; i >= 0; --i) {
-      A = g1x_add(A, t[i]);
-      if (i > 0) {
-        V = g1x_add(V, r[i]);
-        U = g1x_add(U, V);  // adds R_i once for each of its i index steps
+struct ChunkCounts {
+  uint32_t nc0, nc1, ncw;
+};
+
+__host__ __device__ __forceinline__ ChunkCounts chunk_counts(const MsmPlan &p) {
+  ChunkCounts c;
+  c.nc0 = (p.S + kChunk - 1) / kChunk;
+  c.nc1 = (p.S / 2 + kChunk - 1) / kChunk;
+  c.ncw = c.nc0 + p.lgS * c.nc1;
+  return c;
+}
+
+__global__ void __launch_bounds__(kPointThreads)
+    k_msm_bitsums(const g1x *__restrict__ seg_t, const g1x *__restrict__ seg_r, MsmPlan p,
+                  g1x *__restrict__ part) {
+  const ChunkCounts cc = chunk_counts(p);
+  const uint64_t total = (uint64_t)p.W * cc.ncw;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t w = (uint32_t)(t / cc.ncw), u = (uint32_t)(t - (uint64_t)w * cc.ncw);
+    g1x acc = g1x_inf();
+    if (u < cc.nc0) {
+      const g1x *row = seg_t + (uint64_t)w * p.S;
+      const uint32_t lo = u * kChunk, hi = lo + kChunk < p.S ? lo + kChunk : p.S;
+      for (uint32_t i = lo; i < hi; ++i) acc = g1x_add(acc, row[i]);
+    } else {
+      const uint32_t k = (u - cc.nc0) / cc.nc1, ch = (u - cc.nc0) - k * cc.nc1;
+      const g1x *row = seg_r + (uint64_t)w * p.S;
+      const uint32_t half = p.S >> 1;
+      const uint32_t lo = ch * kChunk, hi = lo + kChunk < half ? lo + kChunk : half;
+      for (uint32_t i = lo; i < hi; ++i) {
+        // the i-th segment index with bit k set
+        const uint32_t s = ((i >> k) << (k + 1)) | (1u << k) | (i & ((1u << k) - 1));
+        acc = g1x_add(acc, row[s]);
       }
     }
-    V = g1x_add(V, r[0]);
+    part[t] = acc;
   }
-  sa[k] = A;
-  su[k] = U;
-  sv[k] = V;
+}
+
+// One block per (window, sum): the sum's chunks, then a tree in shared memory.
+// sums[w (1 + lg S) + j].
+constexpr int kReduceThreads = 128;
+
+__global__ void __launch_bounds__(kReduceThreads)
+    k_msm_bitreduce(const g1x *__restrict__ part, MsmPlan p, g1x *__restrict__ sums) {
+  __shared__ g1x red[kReduceThreads];
+  const ChunkCounts cc = chunk_counts(p);
+  const uint32_t L = 1 + p.lgS;
+  const uint32_t w = blockIdx.x / L, j = blockIdx.x - w * L;
+  const uint64_t first = (uint64_t)w * cc.ncw + (j == 0 ? 0 : cc.nc0 + (j - 1) * cc.nc1);
+  const uint32_t cnt = j == 0 ? cc.nc0 : cc.nc1;
+  g1x acc = g1x_inf();
+  for (uint32_t i = threadIdx.x; i < cnt; i += kReduceThreads) acc = g1x_add(acc, part[first + i]);
+  red[threadIdx.x] = acc;
   __syncthreads();
-  uint32_t log_len = 0;  // log2 of the segments a tree node covers
-  for (uint32_t x = m; x > 1; x >>= 1) ++log_len;
-  for (uint32_t h = 1; h < nthr; h <<= 1, ++log_len) {
-    if (k < nthr && (k & (2 * h - 1)) == 0) {
-      sa[k] = g1x_add(sa[k], sa[k + h]);
-      su[k] = g1x_add(g1x_add(su[k], su[k + h]), g1x_dbl_n(sv[k + h], log_len));
-      sv[k] = g1x_add(sv[k], sv[k + h]);
-    }
+  for (uint32_t h = kReduceThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] = g1x_add(red[threadIdx.x], red[threadIdx.x + h]);
     __syncthreads();
   }
-  if (k == 0) {
-    uint32_t log_g = 0;
-    for (uint32_t x = p.G; x > 1; x >>= 1) ++log_g;
-    win[w] = g1x_add(sa[0], g1x_dbl_n(su[0], log_g));
-  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = red[0];
 }
 
 // ---- final Horner chain in one warp.  Every lane holds the same point; the
@@ -449,6 +487,18 @@ __device__ g1x add_warp(const g1x &p, const g1x &q) {
   return o;
 }
 
+// One warp per window: win[w] = sum_s T_s + G sum_k 2^k Q_k (Horner over k)
+__global__ void __launch_bounds__(32) k_msm_wincombine(const g1x *__restrict__ sums, MsmPlan p,
+                                                       g1x *__restrict__ win) {
+  const uint32_t w = blockIdx.x;
+  const g1x *q = sums + (uint64_t)w * (1 + p.lgS);  // q[0] = sum T, q[1 + k] = Q_k
+  g1x acc = p.lgS ? q[p.lgS] : g1x_inf();
+  for (int k = (int)p.lgS - 2; k >= 0; --k) acc = add_warp(dbl_warp(acc), q[1 + k]);
+  for (uint32_t i = 0; i < p.lgG; ++i) acc = dbl_warp(acc);
+  acc = add_warp(acc, q[0]);
+  if (threadIdx.x == 0) win[w] = acc;
+}
+
 // Horner over the windows (one warp), then affine; out = Jacobian (x, y, 1),
 // or all zero for the point at infinity
 __global__ void __launch_bounds__(32) k_msm_final(const g1x *__restrict__ win, MsmPlan p,
@@ -468,7 +518,7 @@ __global__ void __launch_bounds__(32) k_msm_final(const g1x *__restrict__ win, M
 
 struct MsmLayout {
   size_t digits, counts, offsets, cursor, list, groups, goff, next[2], noff[2], part[2], buckets,
-      seg_t, seg_r, win, tiles, total;
+      seg_t, seg_r, chunks, sums, win, tiles, total;
   uint64_t part_cap;  // partial sums one level can leave
   uint32_t levels;    // group levels: K^levels >= n
 };
@@ -499,6 +549,8 @@ MsmLayout msm_layout(uint64_t n, const MsmPlan &p) {
   L.buckets = o, o += up(nb * sizeof(g1x));
   L.seg_t = o, o += up((size_t)p.W * p.S * sizeof(g1x));
   L.seg_r = o, o += up((size_t)p.W * p.S * sizeof(g1x));
+  L.chunks = o, o += up((size_t)p.W * chunk_counts(p).ncw * sizeof(g1x));
+  L.sums = o, o += up((size_t)p.W * (1 + p.lgS) * sizeof(g1x));
   L.win = o, o += up((size_t)p.W * sizeof(g1x));
   L.tiles = o, o += up(((nb + kScanTile - 1) / kScanTile + 1) * 4);
   L.total = o;
@@ -547,6 +599,7 @@ extern "C" int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n
   uint32_t *cursor = u32(L.cursor), *list = u32(L.list), *groups = u32(L.groups);
   uint32_t *goff = u32(L.goff), *tiles = u32(L.tiles);
   g1x *buckets = pts(L.buckets), *seg_t = pts(L.seg_t), *seg_r = pts(L.seg_r), *win = pts(L.win);
+  g1x *chunks = pts(L.chunks), *sums = pts(L.sums);
   const uint64_t nb = (uint64_t)p.W * p.B;
 
   // 1-3: signed digits, bucket sizes, counting sort of (point, sign) by bucket
@@ -587,8 +640,14 @@ extern "C" int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n
       buckets, p, seg_t, seg_r);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  k_msm_windows<<<p.W, kWindowThreads, 3 * kWindowThreads * sizeof(g1x), s>>>(seg_t, seg_r, p,
-                                                                                 win);
+  k_msm_bitsums<<<grid_for((uint64_t)p.W * chunk_counts(p).ncw, kPointThreads, 16), kPointThreads,
+                  0, s>>>(seg_t, seg_r, p, chunks);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_bitreduce<<<p.W * (1 + p.lgS), kReduceThreads, 0, s>>>(chunks, p, sums);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_wincombine<<<p.W, 32, 0, s>>>(sums, p, win);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   k_msm_final<<<1, 32, 0, s>>>(win, p, static_cast<fq *>(d_out));

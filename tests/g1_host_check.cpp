@@ -88,6 +88,26 @@ int main(int argc, char **argv) {
       bad += std::memcmp(got, want, 96) != 0;
       store_aff(g1x_to_affine(g1x_add_affine(g1x_from_affine(pa), g1a_neg(pa))), got);
       for (int j = 0; j < 12; ++j) bad += got[j] != 0;
+      // the dedicated squaring against the multiply, on the coordinates
+      for (const fq *v : {&pa.x, &pa.y, &pb.x, &pb.y}) {
+        const fq s1 = fq_sqr(*v), s2 = fq_mul(*v, *v);
+        bad += std::memcmp(s1.v, s2.v, 48) != 0;
+      }
+    }
+    // squaring edge values: 0, 1, q - 1, q - 2, all-ones low limbs
+    {
+      fq e[5] = {fq_zero(), fq_one(), fq_zero(), fq_zero(), fq_zero()};
+      const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                              PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+      for (int j = 0; j < 12; ++j) e[2].v[j] = e[3].v[j] = q[j];
+      e[2].v[0] -= 1;
+      e[3].v[0] -= 2;
+      for (int j = 0; j < 11; ++j) e[4].v[j] = 0xffffffffu;
+      e[4].v[11] = q[11] - 1;
+      for (const fq &v : e) {
+        const fq s1 = fq_sqr(v), s2 = fq_mul(v, v);
+        bad += std::memcmp(s1.v, s2.v, 48) != 0;
+      }
     }
     std::printf("mismatches %ld\n", bad);
     return bad ? 1 : 0;
