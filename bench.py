@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--lean", action="store_true",
                     help="device timing only (no e2e, CPU baseline, ops): the profiling case")
     ap.add_argument("--lg", type=int, default=LG_N, help="transform size (profiling of smaller cases)")
-    ap.add_argument("--op", default="ntt", choices=["ntt", "msm", "gate", "perm"],
+    ap.add_argument("--op", default="ntt", choices=["ntt", "msm", "gate", "perm", "gpperm", "scans"],
                     help="with --lean: time one operator alone at 2^lg points (profiling case)")
     return ap.parse_args()
 
@@ -455,8 +455,10 @@ def constraint_bench(pp, torch, rate, res):
 
 
 def profile_op(args, pp, torch):
-    """--lean --op msm|gate|perm: one operator at 2^lg points, device time
-    only (the profiling case for ncu launch lists of those kernels)."""
+    """--lean --op msm|gate|perm|gpperm|scans: one operator at 2^lg points,
+    device time only (the profiling case for ncu launch lists of those
+    kernels).  gpperm is the copy-constraint grand product; scans is one
+    grand product, one evaluation and one division by (X + c)."""
     import numpy as np
 
     ppfr = pp.ppfr
@@ -475,6 +477,24 @@ def profile_op(args, pp, torch):
         S = {k: ppfr.random_fr(1, 0x80 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
         out = ppfr.empty(n)
         fn = lambda: ppfr.gate_constraint(V, S, 5, out=out)  # noqa: E731
+    elif args.op == "gpperm":
+        w = [ppfr.random_fr(n, 0xA0 + j) for j in range(3)]
+        sig = [ppfr.random_fr(n, 0xA8 + j) for j in range(3)]
+        params = ppfr.random_fr(5, 0xAF)
+        out = ppfr.empty(n)
+        fn = lambda: ppfr.gp_perm(w, sig, params, out=out)  # noqa: E731
+    elif args.op == "scans":
+        x = ppfr.random_fr(n, 0xB0)
+        pt = ppfr.random_fr(1, 0xB1)
+        y = ppfr.empty(1)
+        work = ppfr.empty(n)
+
+        def fn():
+            work.copy_(x)
+            ppfr.gp_prefix_(work)
+            ppfr.evaluate(x, pt, out=y)
+            work.copy_(x)
+            ppfr.div_xplusc_(work, pt)
     else:
         vec = [ppfr.random_fr(n, 0xC0 + i) for i in range(13)]
         sca = [ppfr.random_fr(1, 0xD0 + i) for i in range(7)]

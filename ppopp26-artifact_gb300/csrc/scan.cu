@@ -240,19 +240,25 @@ struct PermArgs {
   const fr *sigma[3];
   const fr *params;     // beta, gamma, k1, k2, k3
   const fr *omega_pow;  // w^i, i < n
-  fr *z;                // output; holds the numerators, then the ratios
+  fr *z;                // output; holds the numerators until the last pass
   fr *den;              // scratch: denominators
-  fr *pre;              // scratch: running products of the denominators
 };
 
-// Copy-constraint ratios with Montgomery's simultaneous inversion (one field
-// inversion per block of 256*K rows), then the local stage of the prefix
-// product over the ratios (k_gp_apply finishes it).
-__global__ void __launch_bounds__(kScanThreads) k_perm_local(const PermArgs a, ScanGeom g,
-                                                              fr *__restrict__ thread_excl,
-                                                              fr *__restrict__ block_total) {
+// Copy-constraint grand product z_i = prod_{j<i} num_j / den_j, computed as
+//   z_i = (prod_{j<i} num_j) * (prod_{j>=i} den_j) / (prod_j den_j):
+// a prefix product of the numerators and a suffix product of the
+// denominators, both blocked scans, and one field inversion for the whole
+// vector instead of one per block.  A zero denominator makes its ratio 0
+// (num := 0, den := 1), the field-inverse-of-zero-is-zero convention.
+//
+// Pass 1: numerators and denominators; each thread's chunk products; their
+// in-block exclusive prefix (numerators) and exclusive suffix (denominators);
+// the block totals.
+__global__ void __launch_bounds__(kScanThreads, 2)
+    k_perm_local(const PermArgs a, ScanGeom g, fr *__restrict__ thread_num,
+                 fr *__restrict__ thread_den, fr *__restrict__ block_num,
+                 fr *__restrict__ block_den) {
   __shared__ fr s1[kScanThreads], s2[kScanThreads];
-  __shared__ fr s_inv;
   const fr beta = ld_fr(a.params), gamma = ld_fr(a.params + 1);
   const fr bk0 = fr_mul(beta, ld_fr(a.params + 2));
   const fr bk1 = fr_mul(beta, ld_fr(a.params + 3));
@@ -260,7 +266,7 @@ __global__ void __launch_bounds__(kScanThreads) k_perm_local(const PermArgs a, S
   const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
   const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
-  fr D = fr_one();
+  fr N = fr_one(), D = fr_one();
   for (uint64_t i = lo; i < hi; ++i) {
     const fr wi = ld_fr(a.omega_pow + i);
     const fr x0 = ld_fr(a.w[0] + i), x1 = ld_fr(a.w[1] + i), x2 = ld_fr(a.w[2] + i);
@@ -270,39 +276,79 @@ __global__ void __launch_bounds__(kScanThreads) k_perm_local(const PermArgs a, S
     fr den = fr_add(fr_add(x0, fr_mul(beta, ld_fr(a.sigma[0] + i))), gamma);
     den = fr_mul(den, fr_add(fr_add(x1, fr_mul(beta, ld_fr(a.sigma[1] + i))), gamma));
     den = fr_mul(den, fr_add(fr_add(x2, fr_mul(beta, ld_fr(a.sigma[2] + i))), gamma));
+    if (fr_is_zero(den)) {
+      num = fr_zero();
+      den = fr_one();
+    }
     st_fr(a.z + i, num);
     st_fr(a.den + i, den);
-    st_fr(a.pre + i, D);
-    if (!fr_is_zero(den)) D = fr_mul(D, den);
+    N = fr_mul(N, num);
+    D = fr_mul(D, den);
   }
-  // invert every thread's D with one inversion per block
-  const fr Q = block_prefix_product(D, s1);  // s1[t] = D_0..D_t
-  const fr U = block_suffix_product(D, s2);  // s2[t] = D_t..D_last
-  (void)Q;
-  (void)U;
-  if (threadIdx.x == 0) s_inv = fr_inv_binary(s1[blockDim.x - 1]);
+  const fr incl_n = block_prefix_product(N, s1);  // s1[t] = N_0 .. N_t
+  const fr incl_d = block_suffix_product(D, s2);  // s2[t] = D_t .. D_last
+  if (gt < g.threads) {
+    st_fr(thread_num + gt, threadIdx.x ? s1[threadIdx.x - 1] : fr_one());
+    st_fr(thread_den + gt, threadIdx.x + 1 < blockDim.x ? s2[threadIdx.x + 1] : fr_one());
+  }
+  if (threadIdx.x == blockDim.x - 1) st_fr(block_num + blockIdx.x, incl_n);
+  if (threadIdx.x == 0) st_fr(block_den + blockIdx.x, incl_d);
+}
+
+// Pass 2, one block: in place, block_num[b] := the product of the numerator
+// totals of the blocks before b, block_den[b] := the product of the
+// denominator totals of the blocks after b, divided by all denominators.
+__global__ void __launch_bounds__(kScanThreads) k_perm_carry(fr *block_num, fr *block_den,
+                                                              uint32_t nb) {
+  __shared__ fr s1[kScanThreads], s2[kScanThreads];
+  __shared__ fr s_inv;
+  const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+  const uint32_t lo = threadIdx.x * per < nb ? threadIdx.x * per : nb;
+  const uint32_t hi = lo + per < nb ? lo + per : nb;
+  fr N = fr_one(), D = fr_one();
+  for (uint32_t b = lo; b < hi; ++b) {
+    N = fr_mul(N, ld_fr(block_num + b));
+    D = fr_mul(D, ld_fr(block_den + b));
+  }
+  block_prefix_product(N, s1);
+  block_suffix_product(D, s2);  // s2[0]: every denominator (none is zero)
+  if (threadIdx.x == 0) s_inv = fr_inv_binary(s2[0]);
   __syncthreads();
-  fr acc = s_inv;
-  if (threadIdx.x > 0) acc = fr_mul(acc, s1[threadIdx.x - 1]);
-  if (threadIdx.x + 1 < blockDim.x) acc = fr_mul(acc, s2[threadIdx.x + 1]);
-  // acc = D^-1; walk back through the chunk
-  fr P = fr_one();
+  fr run_n = threadIdx.x ? s1[threadIdx.x - 1] : fr_one();
+  fr run_d = fr_mul(s_inv, threadIdx.x + 1 < blockDim.x ? s2[threadIdx.x + 1] : fr_one());
+  for (uint32_t b = lo; b < hi; ++b) {
+    const fr v = ld_fr(block_num + b);
+    st_fr(block_num + b, run_n);
+    run_n = fr_mul(run_n, v);
+  }
+  for (uint32_t b = hi; b > lo; --b) {
+    const fr v = ld_fr(block_den + b - 1);
+    st_fr(block_den + b - 1, run_d);
+    run_d = fr_mul(run_d, v);
+  }
+}
+
+// Pass 3: z_i = (numerators before i) * (denominators from i on) / (all):
+// forward over the chunk for the first factor (kept in z), backward for the
+// second.
+__global__ void __launch_bounds__(kScanThreads)
+    k_perm_apply(const PermArgs a, ScanGeom g, const fr *__restrict__ thread_num,
+                 const fr *__restrict__ thread_den, const fr *__restrict__ block_num,
+                 const fr *__restrict__ block_den) {
+  const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
+  if (gt >= g.threads) return;
+  const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
+  fr run = fr_mul(ld_fr(block_num + blockIdx.x), ld_fr(thread_num + gt));
+  for (uint64_t i = lo; i < hi; ++i) {
+    const fr v = ld_fr(a.z + i);
+    st_fr(a.z + i, run);
+    run = fr_mul(run, v);
+  }
+  run = fr_mul(ld_fr(block_den + blockIdx.x), ld_fr(thread_den + gt));
   for (uint64_t i = hi; i > lo; --i) {
-    const fr d = ld_fr(a.den + i - 1);
-    fr r = fr_zero();
-    if (!fr_is_zero(d)) {
-      const fr inv_d = fr_mul(acc, ld_fr(a.pre + i - 1));
-      acc = fr_mul(acc, d);
-      r = fr_mul(ld_fr(a.z + i - 1), inv_d);
-    }
-    st_fr(a.z + i - 1, r);
-    P = fr_mul(P, r);
+    run = fr_mul(run, ld_fr(a.den + i - 1));
+    st_fr(a.z + i - 1, fr_mul(ld_fr(a.z + i - 1), run));
   }
-  __syncthreads();
-  const fr incl = block_prefix_product(P, s1);
-  const fr excl = threadIdx.x ? s1[threadIdx.x - 1] : fr_one();
-  if (gt < g.threads) st_fr(thread_excl + gt, excl);
-  if (threadIdx.x == blockDim.x - 1) st_fr(block_total + blockIdx.x, incl);
 }
 
 // --------------------------------------------- backward affine recurrence
@@ -511,7 +557,7 @@ extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, co
   const fr *omega_pow = pp::pow_table(pp::host_root_of_unity((int)lg_n, false), lg_n, &st);
   if (st) return st;
   fr *ws = static_cast<fr *>(
-      pp::workspace_get((2 * n + g.threads + g.blocks) * sizeof(fr), s, 1, &st));
+      pp::workspace_get((n + 2 * g.threads + 2 * g.blocks) * sizeof(fr), s, 1, &st));
   if (st) return st;
   pp::PermArgs a;
   for (int j = 0; j < 3; ++j) {
@@ -522,13 +568,17 @@ extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, co
   a.omega_pow = omega_pow;
   a.z = static_cast<fr *>(d_z);
   a.den = ws;
-  a.pre = ws + n;
-  fr *thread_excl = ws + 2 * n, *block_total = thread_excl + g.threads;
-  pp::k_perm_local<<<g.blocks, pp::kScanThreads, 0, s>>>(a, g, thread_excl, block_total);
+  fr *thread_num = ws + n, *thread_den = thread_num + g.threads;
+  fr *block_num = thread_den + g.threads, *block_den = block_num + g.blocks;
+  pp::k_perm_local<<<g.blocks, pp::kScanThreads, 0, s>>>(a, g, thread_num, thread_den, block_num,
+                                                         block_den);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gp_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a.z, a.z, nullptr, g, thread_excl,
-                                                       block_total);
+  pp::k_perm_carry<<<1, pp::kScanThreads, 0, s>>>(block_num, block_den, g.blocks);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_perm_apply<<<g.blocks, pp::kScanThreads, 0, s>>>(a, g, thread_num, thread_den, block_num,
+                                                         block_den);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
