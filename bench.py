@@ -141,6 +141,26 @@ def profile_traffic(name: str):
     return None
 
 
+def reduce_max_over_ranks(values, dist, device):
+    """Element-wise maximum of this rank's timings (ms) over all ranks: the
+    slowest rank sets every whole-job rate.  dist is torch.distributed (or
+    None for one process); device is where the backend reduces ("cuda" for
+    NCCL, "cpu" for gloo)."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def whole_job_rate(elems_per_step, steps, world, ms):
+    """Melem/s of the whole job: every rank transforms its own elems_per_step
+    elements per step (independent replicas), and the slowest rank's ms for
+    `steps` steps is the job's time."""
+    return elems_per_step * steps * world / (ms / 1e3) / 1e6
+
+
 def time_device(fn, steps, warmup, torch):
     """CUDA-event time of `steps` calls of fn() on the current stream (ms total)."""
     for _ in range(warmup):
@@ -300,15 +320,13 @@ def run_ours(args, rank, world, local):
     e2e_direct_ms = time_device(lambda: ppfr.ntt_host(hin, out=hout_d), e2e_steps, 1, torch)
     clk = clocks.stop()
     # max over ranks
-    t = torch.tensor([ms, e2e_ms / e2e_steps * args.steps, e2e_serial_ms / e2e_steps * args.steps,
-                      e2e_direct_ms / e2e_steps * args.steps], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms_norm, e2e_serial_norm, e2e_direct_norm = (float(v) for v in t)
-    value = N * args.steps * world / (ms / 1e3) / 1e6
-    e2e_stream_value = N * args.steps * world / (e2e_ms_norm / 1e3) / 1e6
-    e2e_serial_value = N * args.steps * world / (e2e_serial_norm / 1e3) / 1e6
-    e2e_direct_value = N * args.steps * world / (e2e_direct_norm / 1e3) / 1e6
+    ms, e2e_ms_norm, e2e_serial_norm, e2e_direct_norm = reduce_max_over_ranks(
+        [ms, e2e_ms / e2e_steps * args.steps, e2e_serial_ms / e2e_steps * args.steps,
+         e2e_direct_ms / e2e_steps * args.steps], dist, "cuda")
+    value = whole_job_rate(N, args.steps, world, ms)
+    e2e_stream_value = whole_job_rate(N, args.steps, world, e2e_ms_norm)
+    e2e_serial_value = whole_job_rate(N, args.steps, world, e2e_serial_norm)
+    e2e_direct_value = whole_job_rate(N, args.steps, world, e2e_direct_norm)
     same = torch.equal(hout_d, hout)  # both forms transformed the same input
     if e2e_direct_value >= e2e_stream_value:
         e2e_value, e2e_form = e2e_direct_value, (

@@ -27,7 +27,11 @@ namespace pp {
 // Block scans are work-efficient (Blelloch, "Prefix sums and their
 // applications", 1990): an up-sweep and a down-sweep over a balanced tree,
 // 2(n-1) combines for n = blockDim.x (a power of two) instead of the n log n
-// of a Hillis-Steele scan -- each combine here is one or two field multiplies.
+// of a Hillis-Steele or warp-shuffle scan -- each combine here is one or two
+// field multiplies.  All blocks of these launches are resident at once, so
+// the scans' multiply count, not their depth, is what they cost: warp-shuffle
+// scans (9 dependent steps instead of 16) made the 2^20 grand product,
+// evaluation and division 13-36 % slower on GB300.
 
 // inclusive prefix product over the block (commutative); afterwards s[t]
 // holds thread t's inclusive product, which is also returned
@@ -56,6 +60,74 @@ __device__ fr block_prefix_product(fr v, fr *s) {
   s[t] = incl;
   __syncthreads();
   return incl;
+}
+
+// Warp-shuffle (Kogge-Stone) forms: each warp scans its 32 values in 5
+// steps, then warp 0 scans the warp totals -- 9 dependent multiplies and 3
+// barriers against 16 of each, for about 2.5 times the multiplies.  They win
+// where latency, not multiply throughput, bounds the block: the permutation
+// product's local pass (2 blocks per SM) and its single-block carry pass
+// (2^20: 0.607 -> 0.588 ms).  Afterwards s[t] holds thread t's inclusive
+// prefix (or suffix) product, which is also returned.
+__device__ __forceinline__ fr shfl_up_fr(const fr &v, int o) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_up_sync(0xffffffffu, v.v[i], o);
+  return r;
+}
+__device__ __forceinline__ fr shfl_down_fr(const fr &v, int o) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_down_sync(0xffffffffu, v.v[i], o);
+  return r;
+}
+
+__device__ fr warp_block_prefix_product(fr v, fr *s) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const fr u = shfl_up_fr(v, o);
+    if (lane >= o) v = fr_mul(u, v);
+  }
+  if (lane == 31) s[w] = v;  // warp totals
+  __syncthreads();
+  if (w == 0) {
+    fr x = lane < nw ? s[lane] : fr_one();
+    for (int o = 1; o < nw; o <<= 1) {
+      const fr u = shfl_up_fr(x, o);
+      if (lane >= o) x = fr_mul(u, x);
+    }
+    if (lane < nw) s[lane] = x;  // warps 0 .. lane
+  }
+  __syncthreads();
+  if (w > 0) v = fr_mul(s[w - 1], v);
+  __syncthreads();
+  s[t] = v;
+  __syncthreads();
+  return v;
+}
+
+__device__ fr warp_block_suffix_product(fr v, fr *s) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const fr u = shfl_down_fr(v, o);
+    if (lane + o < 32) v = fr_mul(v, u);
+  }
+  if (lane == 0) s[w] = v;  // warp totals
+  __syncthreads();
+  if (w == 0) {
+    fr x = lane < nw ? s[lane] : fr_one();
+    for (int o = 1; o < nw; o <<= 1) {
+      const fr u = shfl_down_fr(x, o);
+      if (lane + o < nw) x = fr_mul(x, u);
+    }
+    if (lane < nw) s[lane] = x;  // warps lane .. nw-1
+  }
+  __syncthreads();
+  if (w + 1 < nw) v = fr_mul(v, s[w + 1]);
+  __syncthreads();
+  s[t] = v;
+  __syncthreads();
+  return v;
 }
 
 // Suffix composition of affine maps f_t(x) = a_t + b_t x over the block.
@@ -219,22 +291,6 @@ int gp_batch_launch(const GpBatchJob *d_jobs, const uint32_t *d_block_start, uin
   return PP_OK;
 }
 
-// inclusive suffix product over the block
-__device__ fr block_suffix_product(fr v, fr *s) {
-  const int t = threadIdx.x, n = blockDim.x;
-  s[t] = v;
-  __syncthreads();
-  for (int o = 1; o < n; o <<= 1) {
-    fr nv = v;
-    if (t + o < n) nv = fr_mul(v, s[t + o]);
-    __syncthreads();
-    s[t] = nv;
-    v = nv;
-    __syncthreads();
-  }
-  return v;
-}
-
 struct PermArgs {
   const fr *w[3];
   const fr *sigma[3];
@@ -285,8 +341,8 @@ __global__ void __launch_bounds__(kScanThreads, 2)
     N = fr_mul(N, num);
     D = fr_mul(D, den);
   }
-  const fr incl_n = block_prefix_product(N, s1);  // s1[t] = N_0 .. N_t
-  const fr incl_d = block_suffix_product(D, s2);  // s2[t] = D_t .. D_last
+  const fr incl_n = warp_block_prefix_product(N, s1);  // s1[t] = N_0 .. N_t
+  const fr incl_d = warp_block_suffix_product(D, s2);  // s2[t] = D_t .. D_last
   if (gt < g.threads) {
     st_fr(thread_num + gt, threadIdx.x ? s1[threadIdx.x - 1] : fr_one());
     st_fr(thread_den + gt, threadIdx.x + 1 < blockDim.x ? s2[threadIdx.x + 1] : fr_one());
@@ -310,8 +366,8 @@ __global__ void __launch_bounds__(kScanThreads) k_perm_carry(fr *block_num, fr *
     N = fr_mul(N, ld_fr(block_num + b));
     D = fr_mul(D, ld_fr(block_den + b));
   }
-  block_prefix_product(N, s1);
-  block_suffix_product(D, s2);  // s2[0]: every denominator (none is zero)
+  warp_block_prefix_product(N, s1);
+  warp_block_suffix_product(D, s2);  // s2[0]: every denominator (none is zero)
   if (threadIdx.x == 0) s_inv = fr_inv_binary(s2[0]);
   __syncthreads();
   fr run_n = threadIdx.x ? s1[threadIdx.x - 1] : fr_one();
