@@ -137,23 +137,83 @@ PP_HD void fq_row_red(uint32_t t[14]) {
   t[13] = 0;
 }
 
-// One out-of-line copy per translation unit: the point formulas call it
-// ~10-14 times per addition, and with every call inlined the bucket-sum
-// kernels outgrew the instruction cache (instruction-fetch stalls led; the
-// 2^20 MSM ran in 25.5 ms against 18.8 ms with calls).
-#ifdef __CUDACC__
-#define PP_FQ_MUL static __host__ __device__ __noinline__
-#else
-#define PP_FQ_MUL static inline
+// The same rows with bare wide products and two add chains (low words, then
+// high words).  A wide multiply with a 64-bit addend holds the integer-
+// multiply pipe about 1.4 times as long as a bare one; the second add chain
+// runs on the ALU pipe instead.
+PP_HD void fq_row_ab_wide(uint32_t t[14], uint32_t ai, const uint32_t b[12]) {
+  uint32_t lo[12], hi[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) {
+    const uint64_t p = (uint64_t)ai * b[j];
+    lo[j] = (uint32_t)p;
+    hi[j] = (uint32_t)(p >> 32);
+  }
+  t[0] = add_cc(t[0], lo[0]);
+#pragma unroll
+  for (int j = 1; j < 12; ++j) t[j] = addc_cc(t[j], lo[j]);
+  t[12] = addc_cc(t[12], 0);
+  t[13] = addc(t[13], 0);
+  t[1] = add_cc(t[1], hi[0]);
+#pragma unroll
+  for (int j = 1; j < 12; ++j) t[j + 1] = addc_cc(t[j + 1], hi[j]);
+  t[13] = addc(t[13], 0);
+}
+
+PP_HD void fq_row_red_wide(uint32_t t[14]) {
+  const uint32_t q[12] = {PP_Q0, PP_Q1, PP_Q2, PP_Q3, PP_Q4, PP_Q5,
+                          PP_Q6, PP_Q7, PP_Q8, PP_Q9, PP_Q10, PP_Q11};
+  const uint32_t m = t[0] * PP_QP;
+  uint32_t lo[12], hi[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) {
+    const uint64_t p = (uint64_t)m * q[j];
+    lo[j] = (uint32_t)p;
+    hi[j] = (uint32_t)(p >> 32);
+  }
+  (void)add_cc(t[0], lo[0]);  // 0 by the choice of m; keeps the carry
+#pragma unroll
+  for (int j = 1; j < 12; ++j) t[j] = addc_cc(t[j], lo[j]);
+  t[12] = addc_cc(t[12], 0);
+  t[13] = addc(t[13], 0);
+  t[1] = add_cc(t[1], hi[0]);
+#pragma unroll
+  for (int j = 1; j < 12; ++j) t[j + 1] = addc_cc(t[j + 1], hi[j]);
+  t[13] = addc(t[13], 0);
+#pragma unroll
+  for (int k = 0; k < 13; ++k) t[k] = t[k + 1];
+  t[13] = 0;
+}
+
+// Row forms: AB / RED = 0 for the single-chain rows above, 1 for bare wide
+// products.  Every form leaves the same 14-word window after each row.  The
+// MSM's bucket sums keep the integer-multiply pipe ~84 % busy and the ALU
+// pipe ~32 %, so moving the product rows' additions to the ALU pays there:
+// the 2^20 MSM took 15.21 ms with (0, 0), 14.02 with (1, 0), 14.73 with
+// (0, 1) and 14.84 with (1, 1) on GB300.
+#ifndef PP_FQ_AB
+#define PP_FQ_AB 1
 #endif
-PP_FQ_MUL fq fq_mul(const fq &a, const fq &b) {
+#ifndef PP_FQ_RED
+#define PP_FQ_RED 0
+#endif
+// the squaring's product rows: 0 single chain, 1 bare wide products (the
+// same 2^20 MSM time, 14.13 against 14.12 ms)
+#ifndef PP_FQ_SQ_WIDE
+#define PP_FQ_SQ_WIDE 0
+#endif
+
+template <int AB, int RED>
+PP_HD fq fq_mul_rows(const fq &a, const fq &b) {
   uint32_t t[14];
 #pragma unroll
   for (int j = 0; j < 14; ++j) t[j] = 0;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
-    fq_row_ab(t, a.v[i], b.v);
-    fq_row_red(t);
+    if (AB) fq_row_ab_wide(t, a.v[i], b.v);
+    else fq_row_ab(t, a.v[i], b.v);
+    if (RED) fq_row_red_wide(t);
+    else fq_row_red(t);
   }
   // t < 2q < 2^383: t[12] = 0
   fq_reduce_once(t);
@@ -163,6 +223,17 @@ PP_FQ_MUL fq fq_mul(const fq &a, const fq &b) {
   return r;
 }
 
+// One out-of-line copy per translation unit: the point formulas call it
+// ~10-14 times per addition, and with every call inlined the bucket-sum
+// kernels outgrew the instruction cache (instruction-fetch stalls led; the
+// 2^20 MSM ran in 25.5 ms against 18.8 ms with calls).
+#ifdef __CUDACC__
+#define PP_FQ_MUL static __host__ __device__ __noinline__
+#else
+#define PP_FQ_MUL static inline
+#endif
+PP_FQ_MUL fq fq_mul(const fq &a, const fq &b) { return fq_mul_rows<PP_FQ_AB, PP_FQ_RED>(a, b); }
+
 // ---- squaring: a^2 = sum_i a_i C_i 2^(64 i) with C_i = a_i + 2^32 D_i and
 // D_i = 2 floor(a / 2^(32 (i + 1))), so row i multiplies a_i by the 13 - i
 // words of C_i instead of all 12 words of a: 78 wide products instead of 144
@@ -170,6 +241,38 @@ PP_FQ_MUL fq fq_mul(const fq &a, const fq &b) {
 // window has moved i words, so row i's term starts at window word i.
 // A2 = 2a in 13 words; D_i's words are A2[i + 1 ..] with the bit that a_i
 // shifted in cleared.
+// the same row with bare wide products and two add chains
+template <int I>
+PP_HD void fq_row_sq_wide(uint32_t t[14], uint32_t ai, const uint32_t A2[13]) {
+  constexpr int L = I < 11 ? 13 - I : 1;  // words I .. 12 (I = 11: word 11 only)
+  uint32_t lo[13], hi[13];
+  uint64_t p = (uint64_t)ai * ai;
+  lo[0] = (uint32_t)p;
+  hi[0] = (uint32_t)(p >> 32);
+#pragma unroll
+  for (int k = 1; k + 1 < L; ++k) {
+    const uint32_t dk = k == 1 ? (A2[I + 1] & ~1u) : A2[I + k];
+    p = (uint64_t)ai * dk;
+    lo[k] = (uint32_t)p;
+    hi[k] = (uint32_t)(p >> 32);
+  }
+  if constexpr (L > 1) {  // word 12: a_i times the top bit of 2a, no high word
+    lo[L - 1] = A2[12] ? ai : 0u;
+    hi[L - 1] = 0;
+  }
+  t[I] = add_cc(t[I], lo[0]);
+#pragma unroll
+  for (int k = 1; k < L; ++k) t[I + k] = addc_cc(t[I + k], lo[k]);
+#pragma unroll
+  for (int k = I + L; k < 13; ++k) t[k] = addc_cc(t[k], 0);
+  t[13] = addc(t[13], 0);
+  // high words land on I + 1 .. 12 for every row (the select's is 0)
+  t[I + 1] = add_cc(t[I + 1], hi[0]);
+#pragma unroll
+  for (int k = 1; k + 1 < L; ++k) t[I + 1 + k] = addc_cc(t[I + 1 + k], hi[k]);
+  t[13] = addc(t[13], 0);
+}
+
 template <int I>
 PP_HD void fq_row_sq(uint32_t t[14], uint32_t ai, const uint32_t A2[13]) {
   uint32_t lo[13], hi[13];
@@ -202,8 +305,10 @@ PP_HD void fq_row_sq(uint32_t t[14], uint32_t ai, const uint32_t A2[13]) {
 
 template <int I>
 PP_HD void fq_sq_rows(uint32_t t[14], const fq &a, const uint32_t A2[13]) {
-  fq_row_sq<I>(t, a.v[I], A2);
-  fq_row_red(t);
+  if (PP_FQ_SQ_WIDE) fq_row_sq_wide<I>(t, a.v[I], A2);
+  else fq_row_sq<I>(t, a.v[I], A2);
+  if (PP_FQ_RED) fq_row_red_wide(t);
+  else fq_row_red(t);
   if constexpr (I < 11) fq_sq_rows<I + 1>(t, a, A2);
 }
 

@@ -93,6 +93,14 @@ int main(int argc, char **argv) {
         const fq s1 = fq_sqr(*v), s2 = fq_mul(*v, *v);
         bad += std::memcmp(s1.v, s2.v, 48) != 0;
       }
+      // every row form of the multiply gives the same product
+      {
+        const fq m00 = fq_mul_rows<0, 0>(pa.x, pb.y), m01 = fq_mul_rows<0, 1>(pa.x, pb.y);
+        const fq m10 = fq_mul_rows<1, 0>(pa.x, pb.y), m11 = fq_mul_rows<1, 1>(pa.x, pb.y);
+        bad += std::memcmp(m00.v, m01.v, 48) != 0;
+        bad += std::memcmp(m00.v, m10.v, 48) != 0;
+        bad += std::memcmp(m00.v, m11.v, 48) != 0;
+      }
     }
     // squaring edge values: 0, 1, q - 1, q - 2, all-ones low limbs
     {
