@@ -282,7 +282,8 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
             const uint32_t k = ((i & 1) << 2) | (i & 2) | ((i >> 2) & 1);
             x[i] = fr_mul_lazy(x[i], ldg_fr(a.tw_inner + ((c * k) << lgP)));
           }
-        } else if (a.last) {
+        } else if (a.last && a.unit_out) {
+          // the 16-byte store path copies tile words: canonical here
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
         }
@@ -313,7 +314,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
 #pragma unroll
           for (int h = 0; h < 8; h += 2) bfly(x[h], x[h + 1]);
         }
-        if (a.last) {
+        if (a.last && a.unit_out) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
         }
@@ -361,6 +362,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
       if (a.tw_layer) v = fr_mul_lazy(v, ldcs_fr(a.tw_layer + ((uint64_t)o << a.lgS) + col0 + col));
       st_fr(a.out + base + ((uint64_t)o << a.lgS) + col, v);
     } else {
+      v = fr_canon(v);  // one element at a time here, not 8 live in the last round
       if (a.has_post_scale) v = fr_mul(v, a.post_scale);
       const uint64_t g =
           a.P == 1 ? (uint64_t)o : out_base + col + ((uint64_t)o << (a.lgN - a.lgR));
