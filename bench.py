@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--lean", action="store_true",
                     help="device timing only (no e2e, CPU baseline, ops): the profiling case")
     ap.add_argument("--lg", type=int, default=LG_N, help="transform size (profiling of smaller cases)")
-    ap.add_argument("--op", default="ntt", choices=["ntt", "msm", "gate", "perm", "gpperm", "scans"],
+    ap.add_argument("--op", default="ntt",
+                    choices=["ntt", "msm", "msmfixed", "gate", "perm", "gpperm", "scans"],
                     help="with --lean: time one operator alone at 2^lg points (profiling case)")
     return ap.parse_args()
 
@@ -481,15 +482,15 @@ def profile_op(args, pp, torch):
 
     ppfr = pp.ppfr
     n = 1 << args.lg
-    if args.op == "msm":
-        from oracle import oracle as O
-
-        base = O.g1_mul_gen(O.random_fr(1024, 77))
-        reps = max(1, n // 1024)
-        pts = torch.from_numpy(np.ascontiguousarray(np.tile(base, (reps, 1))[:n]).view(np.int64)).cuda()
+    if args.op in ("msm", "msmfixed"):
+        pts = msm_points(ppfr, n)
         sc = ppfr.random_fr(n, 5)
         out = torch.empty((3, 6), dtype=torch.int64, device="cuda")
-        fn = lambda: ppfr.msm_g1(pts, sc, out=out)  # noqa: E731
+        if args.op == "msm":
+            fn = lambda: ppfr.msm_g1(pts, sc, out=out)  # noqa: E731
+        else:
+            bases = ppfr.MsmBases(pts)
+            fn = lambda: bases.msm(sc, out=out)  # noqa: E731
     elif args.op == "gate":
         V = {k: ppfr.random_fr(n, 0x20 + i) for i, k in enumerate(ppfr.GATE_VECTORS)}
         S = {k: ppfr.random_fr(1, 0x80 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
@@ -527,21 +528,26 @@ def profile_op(args, pp, torch):
                       "gpu_launches": int(pp.launch_count() - l0)}), flush=True)
 
 
-def msm_bench(pp, torch, rate, res):
-    """G1 multi-scalar multiplication of 2^20 points.  The points are 1024
-    distinct multiples of the generator (made by the oracle on the host, a
-    set-up step outside the timed region) repeated 1024 times; the scalars are
-    seeded random canonical Fr values.  The bucket method's work does not
-    depend on repeated points.  Integer fraction: W n mixed additions of ~10
-    Fq Montgomery multiplies (W = 256 / c + 1 windows), each 4 * 12^2 = 576
-    32-bit multiply instructions, against the nominal integer peak."""
-    import numpy as np
-    from oracle import oracle as O
+def msm_points(ppfr, n):
+    """n G1 points: 1024 distinct multiples s_i G of the generator (seeded
+    random s_i, made on the device by pp_g1_mul_gen, a set-up step outside
+    any timed region) repeated to n.  The bucket method's work does not
+    depend on repeated points."""
+    base = ppfr.g1_mul_gen(ppfr.random_fr(1024, 77))
+    reps = (n + 1023) // 1024
+    return base.repeat(reps, 1)[:n].contiguous()
 
+
+def msm_bench(pp, torch, rate, res):
+    """G1 multi-scalar multiplication of 2^20 points (msm_points); the
+    scalars are seeded random canonical Fr values.  Integer fraction: W n
+    mixed additions of ~10 Fq Montgomery multiplies (W = 256 / c + 1
+    windows), each 4 * 12^2 = 576 32-bit multiply instructions, against the
+    nominal integer peak.  The fixed-base form times pp_msm_g1_fixed on
+    window tables built once, outside the timed region."""
     ppfr = pp.ppfr
     n = 1 << 20
-    base = O.g1_mul_gen(O.random_fr(1024, 77))
-    pts = torch.from_numpy(np.ascontiguousarray(np.tile(base, (n // 1024, 1))).view(np.int64)).cuda()
+    pts = msm_points(ppfr, n)
     sc = ppfr.random_fr(n, 5)
     out = torch.empty((3, 6), dtype=torch.int64, device="cuda")
     name = "msm_g1_2^20"
@@ -554,6 +560,18 @@ def msm_bench(pp, torch, rate, res):
     res[name].update({"window_bits": c, "windows": windows,
                       "int_frac_of_nominal_peak": round(instr / (res[name]["ms"] / 1e3) / peak, 4),
                       "points": "1024 distinct generator multiples, tiled"})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bases = ppfr.MsmBases(pts)
+    torch.cuda.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    name = "msm_g1_fixed_2^20"
+    rate(name, lambda: bases.msm(sc, out=out), n, 3)
+    same = torch.equal(bases.msm(sc), ppfr.msm_g1(pts, sc))
+    res[name].update({"window_bits": bases.window_bits, "windows": 256 // bases.window_bits + 1,
+                      "table_gb": round(bases.table_bytes / 1e9, 3),
+                      "table_build_ms": round(build_ms, 1), "same_as_plain": bool(same)})
+    bases.close()
 
 
 def batched_bench(pp, torch):

@@ -321,6 +321,40 @@ int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n, void *str
  * points, 4.0 GB for 2^22. */
 int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n, void *d_out, void *stream);
 int pp_msm_g1_window_bits(uint64_t n);
+/* Tuning: the window bits pp_msm_g1 uses for n with ceil(lg n) = lg_n
+ * (0 restores the built-in choice; otherwise 6..20).  Process-wide; the
+ * result does not depend on it. */
+int pp_msm_g1_set_window_bits(uint32_t lg_n, uint32_t window_bits);
+
+/* Fixed-base form of pp_msm_g1, for a point set that many MSMs share (a
+ * prover's commitment key).  No reference counterpart: an addition beside
+ * multi_scalar_mult (PLONK/utils/function.cu:395-411) whose results are the
+ * same bit for bit, for any points and scalars.
+ *
+ * pp_msm_g1_bases_create builds, in HBM, the window tables 2^(c w) P_i
+ * (affine, w < W = 256 / c + 1) of n points: W n 96-byte entries, e.g.
+ * 1.7 GB for 2^20 points at c = 16, 5.2 GB for 2^22 at c = 20.  window_bits
+ * 0 picks c for n; 6..20 sets it.  It reads d_points on `stream` (keep them valid until that work is
+ * done) and allocates with cudaMalloc; W n must stay below 2^31.
+ * pp_msm_g1_fixed then computes sum_i s_i P_i for n scalars like pp_msm_g1:
+ * every window's digits go to one shared set of 2^(c-1) buckets, so the
+ * window sums run once and there is no Horner chain over the windows.  Call
+ * it with the device of the tables current.  pp_msm_g1_bases_destroy frees
+ * the tables (a null handle is fine). */
+typedef struct pp_msm_bases pp_msm_bases;
+int pp_msm_g1_bases_create(const void *d_points, uint64_t n, uint32_t window_bits,
+                           pp_msm_bases **bases, void *stream);
+int pp_msm_g1_bases_destroy(pp_msm_bases *bases);
+int pp_msm_g1_bases_info(const pp_msm_bases *bases, uint64_t *n, uint32_t *window_bits,
+                         uint64_t *table_bytes);
+int pp_msm_g1_fixed(const pp_msm_bases *bases, const void *d_scalars, void *d_out, void *stream);
+
+/* s_i G for the G1 generator G and n plain 256-bit scalars (32 bytes each,
+ * the MSM's scalar format) -> n affine points (96 bytes each, all zero for
+ * infinity), one thread per scalar.  For test and benchmark points and
+ * commitments to known constants; the reference builds such points on the
+ * host with blst.  Buffers 16-byte aligned. */
+int pp_g1_mul_gen(const void *d_scalars, uint64_t n, void *d_out, void *stream);
 
 /* -------------------------------------------------------- data formats ---
  * The reference's element files are raw 32-byte little-endian Montgomery

@@ -19,6 +19,16 @@ struct g1x {
   fq x, y, zz, zzz;
 };
 
+// The group's standard generator, affine, Montgomery form (32-bit limbs, least
+// significant first): the point blst calls BLS12_381_G1, which the MSM tests
+// compare it with.
+PP_HD g1a g1_generator() {
+  return g1a{{{0xfd530c16u, 0x5cb38790u, 0x9976fff5u, 0x7817fc67u, 0x143ba1c1u, 0x154f95c7u,
+                0xf3d0e747u, 0xf0ae6acdu, 0x21dbf440u, 0xedce6eccu, 0x9e0bfb75u, 0x12017741u}},
+             {{0x0ce72271u, 0xbaac93d5u, 0x7918fd8eu, 0x8c22631au, 0x570725ceu, 0xdd595f13u,
+                0x50405194u, 0x51ac5829u, 0xad0059c0u, 0x0e1c8c3fu, 0x5008a26au, 0x0bbc3efcu}}};
+}
+
 PP_HD g1x g1x_inf() {
   g1x p;
   p.x = fq_one();

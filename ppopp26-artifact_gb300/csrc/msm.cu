@@ -30,6 +30,7 @@
 //                inversion to affine
 // Every step is integer-multiply bound (an Fq multiply is ~300 32-bit wide
 // products) except the sort, which is a few bytes per point and window.
+#include <atomic>
 #include <cstring>
 
 #include "common.cuh"
@@ -41,13 +42,14 @@ namespace {
 constexpr uint32_t kNone = 0xffffffffu;
 
 struct MsmPlan {
-  uint32_t c;    // window bits
-  uint32_t W;    // windows: W c >= 257, so the top window's carry has a home
-  uint32_t B;    // buckets per window, 2^(c-1)
-  uint32_t G;    // buckets per aggregation segment
-  uint32_t S;    // segments per window, B / G
-  uint32_t lgG;  // log2 G
-  uint32_t lgS;  // log2 S
+  uint32_t c;      // window bits
+  uint32_t W;      // windows: W c >= 257, so the top window's carry has a home
+  uint32_t B;      // buckets per bucket set, 2^(c-1)
+  uint32_t G;      // buckets per aggregation segment
+  uint32_t S;      // segments per bucket set, B / G
+  uint32_t lgG;    // log2 G
+  uint32_t lgS;    // log2 S
+  uint32_t nsets;  // bucket sets: W (one per window), or 1 with window tables
 };
 
 // Buckets per segment: the longest run (fewer, cheaper window sums) that still
@@ -55,27 +57,61 @@ struct MsmPlan {
 // points: 16 -> 4.65 ms, 4 -> 3.92 ms; 2^22: 4 -> 53.2 ms, 16 -> 51.3 ms).
 constexpr uint32_t kSegmentMax = 16, kSegmentMin = 4, kSegmentThreads = 1u << 15;
 
-// minimise W (10 n + 14 2^c) Fq multiplies: the bucket sums (one mixed add
-// per point and window) against the aggregation (two adds per bucket)
-MsmPlan msm_plan(uint64_t n) {
+// the rest of a plan once c and the number of bucket sets are fixed
+MsmPlan msm_plan_for(uint32_t c, uint32_t nsets) {
   MsmPlan p{};
-  double best = 0;
-  for (uint32_t c = 6; c <= 20; ++c) {
-    const double W = 256 / c + 1;
-    const double cost = W * (10.0 * (double)n + 14.0 * (double)(1u << c));
-    if (p.c == 0 || cost < best) {
-      best = cost;
-      p.c = c;
-    }
-  }
-  p.W = 256 / p.c + 1;
-  p.B = 1u << (p.c - 1);
+  p.c = c;
+  p.W = 256 / c + 1;
+  p.B = 1u << (c - 1);
+  p.nsets = nsets;
   p.G = kSegmentMax;  // B >= 32 (c >= 6)
-  while (p.G > kSegmentMin && (uint64_t)p.W * p.B / p.G < kSegmentThreads) p.G >>= 1;
+  while (p.G > kSegmentMin && (uint64_t)p.nsets * p.B / p.G < kSegmentThreads) p.G >>= 1;
   p.S = p.B / p.G;
   while ((1u << p.lgG) < p.G) ++p.lgG;
   while ((1u << p.lgS) < p.S) ++p.lgS;
   return p;
+}
+
+// per-size window bits set by pp_msm_g1_set_window_bits (index: ceil(lg n))
+std::atomic<uint32_t> g_window_bits[33];
+
+uint32_t ceil_lg(uint64_t n) {
+  uint32_t lg = 0;
+  while (lg < 32 && (1ull << lg) < n) ++lg;
+  return lg;
+}
+
+// Window bits.  Scalars below r < 2^255 leave the top window few digit
+// values unless c is 13, 16 or 20 (the top window then spans 232, 29678 or
+// 29678 values): with other c about n entries share a handful of buckets, or
+// one carry window, and those buckets need extra levels of serial group sums.
+// Swept on GB300 (2^12..2^24 points, c = 10..20), these won: 13 up to 2^19
+// points (2^14: 2.86 ms against 3.45 for the cost model's 11), 16 up to 2^23
+// (2^22: 41.2 against 47.2 for 18), 18 beyond (2^24: 149.8 against 158.6 for
+// 20).  Below 2^10 points the cost model decides.
+//
+// The model minimises W (10 n + 14 2^c) Fq multiplies: the bucket sums (one
+// mixed add per point and window) against the aggregation (two adds per
+// bucket).
+MsmPlan msm_plan(uint64_t n) {
+  const uint32_t lg = ceil_lg(n);
+  const uint32_t forced = g_window_bits[lg].load(std::memory_order_relaxed);
+  if (forced) return msm_plan_for(forced, 256 / forced + 1);
+  if (lg >= 10) {
+    const uint32_t c = lg <= 19 ? 13 : lg <= 23 ? 16 : 18;
+    return msm_plan_for(c, 256 / c + 1);
+  }
+  uint32_t best_c = 0;
+  double best = 0;
+  for (uint32_t c = 6; c <= 20; ++c) {
+    const double W = 256 / c + 1;
+    const double cost = W * (10.0 * (double)n + 14.0 * (double)(1u << c));
+    if (best_c == 0 || cost < best) {
+      best = cost;
+      best_c = c;
+    }
+  }
+  return msm_plan_for(best_c, 256 / best_c + 1);
 }
 
 __device__ __forceinline__ g1a ld_g1a(const g1a *p) {
@@ -140,7 +176,7 @@ __global__ void k_msm_digits(const uint32_t *__restrict__ scalars, uint64_t n, M
       if (mag) {
         const uint32_t bucket = mag - 1;
         e = (bucket << 1) | sign;
-        warp_increment(counts, w * p.B + bucket);
+        warp_increment(counts, (p.nsets > 1 ? w * p.B : 0) + bucket);
       }
       digits[(uint64_t)w * n + i] = e;
     }
@@ -248,6 +284,8 @@ int scan_u32(const uint32_t *in, uint64_t len, uint32_t *out, uint32_t *cursor, 
   return PP_OK;
 }
 
+// With one bucket set per window an entry names its point i; with window
+// tables (one bucket set) it names the table entry w n + i = 2^(c w) P_i.
 __global__ void k_msm_scatter(const uint32_t *__restrict__ digits, uint64_t n, MsmPlan p,
                               uint32_t *__restrict__ cursor, uint32_t *__restrict__ list) {
   const uint64_t total = (uint64_t)p.W * n;
@@ -256,8 +294,9 @@ __global__ void k_msm_scatter(const uint32_t *__restrict__ digits, uint64_t n, M
     const uint32_t e = digits[t];
     if (e == kNone) continue;
     const uint64_t w = t / n, i = t - w * n;
-    const uint32_t pos = warp_increment(cursor, (uint32_t)(w * p.B) + (e >> 1));
-    list[pos] = (uint32_t)i | ((e & 1u) << 31);
+    const bool per_window = p.nsets > 1;
+    const uint32_t pos = warp_increment(cursor, (per_window ? (uint32_t)(w * p.B) : 0u) + (e >> 1));
+    list[pos] = (uint32_t)(per_window ? i : t) | ((e & 1u) << 31);
   }
 }
 
@@ -328,7 +367,7 @@ __global__ void __launch_bounds__(kPointThreads, 3)
 __global__ void __launch_bounds__(kPointThreads)
     k_msm_segments(const g1x *__restrict__ buckets, MsmPlan p, g1x *__restrict__ seg_t,
                    g1x *__restrict__ seg_r) {
-  const uint64_t total = (uint64_t)p.W * p.S;
+  const uint64_t total = (uint64_t)p.nsets * p.S;
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
     const g1x *row = buckets + t * p.G;  // segments are consecutive in each window
@@ -369,7 +408,7 @@ __global__ void __launch_bounds__(kPointThreads)
     k_msm_bitsums(const g1x *__restrict__ seg_t, const g1x *__restrict__ seg_r, MsmPlan p,
                   g1x *__restrict__ part) {
   const ChunkCounts cc = chunk_counts(p);
-  const uint64_t total = (uint64_t)p.W * cc.ncw;
+  const uint64_t total = (uint64_t)p.nsets * cc.ncw;
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t w = (uint32_t)(t / cc.ncw), u = (uint32_t)(t - (uint64_t)w * cc.ncw);
@@ -503,8 +542,8 @@ __global__ void __launch_bounds__(32) k_msm_wincombine(const g1x *__restrict__ s
 // or all zero for the point at infinity
 __global__ void __launch_bounds__(32) k_msm_final(const g1x *__restrict__ win, MsmPlan p,
                                                   fq *__restrict__ out) {
-  g1x acc = win[p.W - 1];
-  for (int w = (int)p.W - 2; w >= 0; --w) {
+  g1x acc = win[p.nsets - 1];
+  for (int w = (int)p.nsets - 2; w >= 0; --w) {
     for (uint32_t k = 0; k < p.c; ++k) acc = dbl_warp(acc);
     acc = add_warp(acc, win[w]);
   }
@@ -520,18 +559,21 @@ struct MsmLayout {
   size_t digits, counts, offsets, cursor, list, groups, goff, next[2], noff[2], part[2], buckets,
       seg_t, seg_r, chunks, sums, win, tiles, total;
   uint64_t part_cap;  // partial sums one level can leave
-  uint32_t levels;    // group levels: K^levels >= n
+  uint32_t levels;    // group levels: K^levels >= the largest bucket
 };
 
 MsmLayout msm_layout(uint64_t n, const MsmPlan &p) {
   MsmLayout L{};
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  const uint64_t nb = (uint64_t)p.W * p.B;
+  const uint64_t nb = (uint64_t)p.nsets * p.B;
   const uint64_t entries = (uint64_t)p.W * n;
   // a bucket of m > K values leaves ceil(m / K) <= 2 m / K partial sums
   L.part_cap = 2 * entries / kGroup + 1;
+  // a bucket holds at most one entry per point and window: n with a bucket
+  // set per window, W n when all windows share one
+  const uint64_t largest = p.nsets > 1 ? n : entries;
   L.levels = 1;
-  for (uint64_t span = kGroup; span < n; span *= kGroup) ++L.levels;
+  for (uint64_t span = kGroup; span < largest; span *= kGroup) ++L.levels;
   size_t o = 0;
   L.digits = o, o += up(entries * 4);
   L.counts = o, o += up(nb * 4);
@@ -547,11 +589,11 @@ MsmLayout msm_layout(uint64_t n, const MsmPlan &p) {
   L.part[0] = o, o += up(L.part_cap * sizeof(g1x));
   L.part[1] = o, o += up(L.part_cap * sizeof(g1x));
   L.buckets = o, o += up(nb * sizeof(g1x));
-  L.seg_t = o, o += up((size_t)p.W * p.S * sizeof(g1x));
-  L.seg_r = o, o += up((size_t)p.W * p.S * sizeof(g1x));
-  L.chunks = o, o += up((size_t)p.W * chunk_counts(p).ncw * sizeof(g1x));
-  L.sums = o, o += up((size_t)p.W * (1 + p.lgS) * sizeof(g1x));
-  L.win = o, o += up((size_t)p.W * sizeof(g1x));
+  L.seg_t = o, o += up((size_t)p.nsets * p.S * sizeof(g1x));
+  L.seg_r = o, o += up((size_t)p.nsets * p.S * sizeof(g1x));
+  L.chunks = o, o += up((size_t)p.nsets * chunk_counts(p).ncw * sizeof(g1x));
+  L.sums = o, o += up((size_t)p.nsets * (1 + p.lgS) * sizeof(g1x));
+  L.win = o, o += up((size_t)p.nsets * sizeof(g1x));
   L.tiles = o, o += up(((nb + kScanTile - 1) / kScanTile + 1) * 4);
   L.total = o;
   return L;
@@ -561,6 +603,137 @@ unsigned grid_for(uint64_t work, int threads, int per_sm) {
   const uint64_t want = (work + threads - 1) / threads;
   const uint64_t cap = (uint64_t)device_sm_count() * per_sm;
   return (unsigned)(want < cap ? (want ? want : 1) : cap);
+}
+
+// ---- window tables of a fixed point set: table[w n + i] = 2^(c w) P_i in
+// affine form.  Window w + 1 comes from window w by c doublings in XYZZ and a
+// batched conversion back to affine: Montgomery's simultaneous inversion over
+// runs of kTableRun points, one field inversion per run.
+constexpr uint32_t kTableRun = 32;
+
+__global__ void __launch_bounds__(kPointThreads)
+    k_msm_table_double(const g1a *__restrict__ prev, uint64_t n, uint32_t c, g1x *__restrict__ out) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    g1x q = g1x_dbl_affine(ld_g1a(prev + i));
+    for (uint32_t k = 1; k < c; ++k) q = g1x_dbl(q);
+    out[i] = q;
+  }
+}
+
+// x = X / ZZ, y = Y / ZZZ with 1 / (ZZ ZZZ) from the run's one inversion; the
+// forward pass parks the running products in out[].x, the backward pass reads
+// each one before it overwrites it.  Infinity (ZZ = 0) becomes all zero.
+__global__ void __launch_bounds__(kPointThreads)
+    k_msm_table_affine(const g1x *__restrict__ q, uint64_t n, g1a *__restrict__ out) {
+  const uint64_t runs = (n + kTableRun - 1) / kTableRun;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < runs;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t lo = r * kTableRun, hi = lo + kTableRun < n ? lo + kTableRun : n;
+    fq acc = fq_one();
+    for (uint64_t j = lo; j < hi; ++j) {
+      const g1x p = q[j];
+      if (!g1x_is_inf(p)) acc = fq_mul(acc, fq_mul(p.zz, p.zzz));
+      out[j].x = acc;
+    }
+    fq inv = fq_inv(acc);  // acc is a product of non-zero values
+    for (uint64_t j = hi; j > lo; --j) {
+      const g1x p = q[j - 1];
+      g1a a;
+      if (g1x_is_inf(p)) {
+        a.x = fq_zero();
+        a.y = fq_zero();
+      } else {
+        const fq before = j - 1 > lo ? out[j - 2].x : fq_one();
+        const fq inv_d = fq_mul(inv, before);  // 1 / (ZZ ZZZ) of this point
+        inv = fq_mul(inv, fq_mul(p.zz, p.zzz));
+        a.x = fq_mul(p.x, fq_mul(inv_d, p.zzz));
+        a.y = fq_mul(p.y, fq_mul(inv_d, p.zz));
+      }
+      out[j - 1] = a;
+    }
+  }
+}
+
+// Window bits for a fixed point set, from the same kind of sweep (c = 12..20,
+// 2^14..2^24 points on GB300) and the same top-window effect: 13 up to 2^14
+// points, 16 up to 2^21 (2^20: 10.72 ms against 10.98 for 17 and 11.83 for
+// 15), 20 beyond (2^22: 33.8 against 35.8 for 19).  One bucket set serves all
+// windows, so a large c costs little aggregation.
+uint32_t fixed_window_bits(uint64_t n) {
+  const uint32_t lg = ceil_lg(n);
+  return lg <= 14 ? 13 : lg <= 21 ? 16 : 20;
+}
+
+// The pipeline behind both entry points.  points holds n affine points (one
+// bucket set per window) or the W n window-table entries (one bucket set);
+// scalars n plain 256-bit integers; out receives (x, y, 1), or zeros.
+int msm_run(const g1a *points, const uint32_t *scalars, uint64_t n, const MsmPlan &p, fq *out,
+            cudaStream_t s) {
+  const MsmLayout L = msm_layout(n, p);
+  int st = PP_OK;
+  char *ws = static_cast<char *>(workspace_get(L.total, s, 3, &st));
+  if (st) return st;
+  auto u32 = [&](size_t off) { return reinterpret_cast<uint32_t *>(ws + off); };
+  auto pts = [&](size_t off) { return reinterpret_cast<g1x *>(ws + off); };
+  uint32_t *digits = u32(L.digits), *counts = u32(L.counts), *offsets = u32(L.offsets);
+  uint32_t *cursor = u32(L.cursor), *list = u32(L.list), *groups = u32(L.groups);
+  uint32_t *goff = u32(L.goff), *tiles = u32(L.tiles);
+  g1x *buckets = pts(L.buckets), *seg_t = pts(L.seg_t), *seg_r = pts(L.seg_r), *win = pts(L.win);
+  g1x *chunks = pts(L.chunks), *sums = pts(L.sums);
+  const uint64_t nb = (uint64_t)p.nsets * p.B;
+
+  // 1-3: signed digits, bucket sizes, counting sort of (point, sign) by bucket
+  PP_CUDA_TRY(cudaMemsetAsync(counts, 0, nb * 4, s));
+  k_msm_digits<<<grid_for(n, 256, 8), 256, 0, s>>>(scalars, n, p, digits, counts);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  if ((st = scan_u32(counts, nb, offsets, cursor, tiles, s))) return st;
+  k_msm_scatter<<<grid_for((uint64_t)p.W * n, 256, 8), 256, 0, s>>>(digits, n, p, cursor, list);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+
+  // 4: bucket sums, at most K values per thread, over L.levels levels
+  PP_CUDA_TRY(cudaMemsetAsync(buckets, 0, nb * sizeof(g1x), s));  // all zero = infinity
+  const uint32_t *m = counts, *off = offsets;
+  const g1x *part_in = nullptr;
+  for (uint32_t lv = 0; lv < L.levels; ++lv) {
+    uint32_t *next = u32(L.next[lv & 1]), *noff = u32(L.noff[lv & 1]);
+    g1x *part_out = pts(L.part[lv & 1]);
+    k_msm_groups<<<grid_for(nb, 256, 8), 256, 0, s>>>(m, nb, groups, next);
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    if ((st = scan_u32(groups, nb, goff, nullptr, tiles, s))) return st;
+    if ((st = scan_u32(next, nb, noff, nullptr, tiles, s))) return st;
+    k_msm_level<<<grid_for((uint64_t)p.W * n / 4 + nb, kPointThreads, 16), kPointThreads, 0, s>>>(
+        points, lv == 0 ? list : nullptr, part_in, m, off, goff, noff,
+        (uint32_t)nb, part_out, buckets);
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    m = next;
+    off = noff;
+    part_in = part_out;
+  }
+
+  // 5-7: weighted bucket sums per bucket set, sets combined, affine result
+  k_msm_segments<<<grid_for((uint64_t)p.nsets * p.S, kPointThreads, 16), kPointThreads, 0, s>>>(
+      buckets, p, seg_t, seg_r);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_bitsums<<<grid_for((uint64_t)p.nsets * chunk_counts(p).ncw, kPointThreads, 16), kPointThreads,
+                  0, s>>>(seg_t, seg_r, p, chunks);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_bitreduce<<<p.nsets * (1 + p.lgS), kReduceThreads, 0, s>>>(chunks, p, sums);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_wincombine<<<p.nsets, 32, 0, s>>>(sums, p, win);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  k_msm_final<<<1, 32, 0, s>>>(win, p, out);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  return PP_OK;
 }
 
 }  // namespace
@@ -589,71 +762,181 @@ extern "C" int pp_msm_g1(const void *d_points, const void *d_scalars, uint64_t n
               (unsigned long long)n);
     return PP_E_UNSUPPORTED;
   }
-  const MsmLayout L = msm_layout(n, p);
-  int st = PP_OK;
-  char *ws = static_cast<char *>(workspace_get(L.total, s, 3, &st));
-  if (st) return st;
-  auto u32 = [&](size_t off) { return reinterpret_cast<uint32_t *>(ws + off); };
-  auto pts = [&](size_t off) { return reinterpret_cast<g1x *>(ws + off); };
-  uint32_t *digits = u32(L.digits), *counts = u32(L.counts), *offsets = u32(L.offsets);
-  uint32_t *cursor = u32(L.cursor), *list = u32(L.list), *groups = u32(L.groups);
-  uint32_t *goff = u32(L.goff), *tiles = u32(L.tiles);
-  g1x *buckets = pts(L.buckets), *seg_t = pts(L.seg_t), *seg_r = pts(L.seg_r), *win = pts(L.win);
-  g1x *chunks = pts(L.chunks), *sums = pts(L.sums);
-  const uint64_t nb = (uint64_t)p.W * p.B;
+  return msm_run(static_cast<const g1a *>(d_points), static_cast<const uint32_t *>(d_scalars), n, p,
+                 static_cast<fq *>(d_out), s);
+}
 
-  // 1-3: signed digits, bucket sizes, counting sort of (point, sign) by bucket
-  PP_CUDA_TRY(cudaMemsetAsync(counts, 0, nb * 4, s));
-  k_msm_digits<<<grid_for(n, 256, 8), 256, 0, s>>>(static_cast<const uint32_t *>(d_scalars), n, p,
-                                                    digits, counts);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  if ((st = scan_u32(counts, nb, offsets, cursor, tiles, s))) return st;
-  k_msm_scatter<<<grid_for((uint64_t)p.W * n, 256, 8), 256, 0, s>>>(digits, n, p, cursor, list);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
+extern "C" int pp_msm_g1_window_bits(uint64_t n) { return (int)pp::msm_plan(n).c; }
 
-  // 4: bucket sums, at most K values per thread, over L.levels levels
-  PP_CUDA_TRY(cudaMemsetAsync(buckets, 0, nb * sizeof(g1x), s));  // all zero = infinity
-  const uint32_t *m = counts, *off = offsets;
-  const g1x *part_in = nullptr;
-  for (uint32_t lv = 0; lv < L.levels; ++lv) {
-    uint32_t *next = u32(L.next[lv & 1]), *noff = u32(L.noff[lv & 1]);
-    g1x *part_out = pts(L.part[lv & 1]);
-    k_msm_groups<<<grid_for(nb, 256, 8), 256, 0, s>>>(m, nb, groups, next);
-    PP_COUNT_LAUNCH();
-    PP_LAUNCH_CHECK();
-    if ((st = scan_u32(groups, nb, goff, nullptr, tiles, s))) return st;
-    if ((st = scan_u32(next, nb, noff, nullptr, tiles, s))) return st;
-    k_msm_level<<<grid_for((uint64_t)p.W * n / 4 + nb, kPointThreads, 16), kPointThreads, 0, s>>>(
-        static_cast<const g1a *>(d_points), lv == 0 ? list : nullptr, part_in, m, off, goff, noff,
-        (uint32_t)nb, part_out, buckets);
-    PP_COUNT_LAUNCH();
-    PP_LAUNCH_CHECK();
-    m = next;
-    off = noff;
-    part_in = part_out;
+extern "C" int pp_msm_g1_set_window_bits(uint32_t lg_n, uint32_t window_bits) {
+  if (lg_n > 32 || (window_bits && (window_bits < 6 || window_bits > 20))) {
+    pp::set_error("pp_msm_g1_set_window_bits: lg_n <= 32 and window_bits 0 or 6..20");
+    return PP_E_INVAL;
   }
+  pp::g_window_bits[lg_n].store(window_bits, std::memory_order_relaxed);
+  return PP_OK;
+}
 
-  // 5-7: weighted bucket sums per window, windows combined, affine result
-  k_msm_segments<<<grid_for((uint64_t)p.W * p.S, kPointThreads, 16), kPointThreads, 0, s>>>(
-      buckets, p, seg_t, seg_r);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  k_msm_bitsums<<<grid_for((uint64_t)p.W * chunk_counts(p).ncw, kPointThreads, 16), kPointThreads,
-                  0, s>>>(seg_t, seg_r, p, chunks);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  k_msm_bitreduce<<<p.W * (1 + p.lgS), kReduceThreads, 0, s>>>(chunks, p, sums);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  k_msm_wincombine<<<p.W, 32, 0, s>>>(sums, p, win);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  k_msm_final<<<1, 32, 0, s>>>(win, p, static_cast<fq *>(d_out));
+// ---- fixed-base form: the window tables of one point set stay in HBM ----
+struct pp_msm_bases {
+  int device;
+  uint64_t n;
+  uint32_t c;
+  pp::g1a *table;  // W n affine points, table[w n + i] = 2^(c w) P_i
+};
+
+extern "C" int pp_msm_g1_bases_create(const void *d_points, uint64_t n, uint32_t window_bits,
+                                      pp_msm_bases **bases, void *stream) {
+  using namespace pp;
+  if (!bases) {
+    set_error("pp_msm_g1_bases_create: null handle pointer");
+    return PP_E_INVAL;
+  }
+  *bases = nullptr;
+  if (!d_points || (reinterpret_cast<uintptr_t>(d_points) & 15)) {
+    set_error("pp_msm_g1_bases_create: points must be a 16-byte aligned device pointer");
+    return PP_E_INVAL;
+  }
+  if (n == 0 || (window_bits && (window_bits < 6 || window_bits > 20))) {
+    set_error("pp_msm_g1_bases_create: need n >= 1 and window_bits 0 (automatic) or 6..20");
+    return PP_E_INVAL;
+  }
+  const uint32_t c = window_bits ? window_bits : fixed_window_bits(n);
+  const uint64_t W = 256 / c + 1;
+  if (W * n >= (1ull << 31)) {
+    set_error("pp_msm_g1_bases_create: %llu windows x %llu points exceed 2^31 table entries",
+              (unsigned long long)W, (unsigned long long)n);
+    return PP_E_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  g1a *table = nullptr;
+  if (cudaMalloc(&table, W * n * sizeof(g1a)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("pp_msm_g1_bases_create: cannot allocate %llu bytes of window tables",
+              (unsigned long long)(W * n * sizeof(g1a)));
+    return PP_E_NOMEM;
+  }
+  g1x *tmp = nullptr;
+  if (cudaMallocAsync(&tmp, n * sizeof(g1x), s) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(table);
+    set_error("pp_msm_g1_bases_create: cannot allocate %llu bytes of scratch",
+              (unsigned long long)(n * sizeof(g1x)));
+    return PP_E_NOMEM;
+  }
+  int st = PP_OK;
+  if (cudaMemcpyAsync(table, d_points, n * sizeof(g1a), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+    st = PP_E_CUDA;
+    set_error("pp_msm_g1_bases_create: copying the points failed: %s",
+              cudaGetErrorString(cudaGetLastError()));
+  }
+  for (uint64_t w = 1; st == PP_OK && w < W; ++w) {
+    k_msm_table_double<<<grid_for(n, kPointThreads, 16), kPointThreads, 0, s>>>(table + (w - 1) * n,
+                                                                               n, c, tmp);
+    PP_COUNT_LAUNCH();
+    k_msm_table_affine<<<grid_for((n + kTableRun - 1) / kTableRun, kPointThreads, 16), kPointThreads,
+                         0, s>>>(tmp, n, table + w * n);
+    PP_COUNT_LAUNCH();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      st = PP_E_CUDA;
+      set_error("pp_msm_g1_bases_create: kernel launch failed: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaFreeAsync(tmp, s);
+  if (st) {
+    cudaFree(table);
+    return st;
+  }
+  *bases = new pp_msm_bases{dev, n, c, table};
+  return PP_OK;
+}
+
+extern "C" int pp_msm_g1_bases_destroy(pp_msm_bases *bases) {
+  if (!bases) return PP_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(bases->device);
+  const cudaError_t e = cudaFree(bases->table);
+  cudaSetDevice(cur);
+  delete bases;
+  if (e != cudaSuccess) {
+    pp::set_error("pp_msm_g1_bases_destroy: cudaFree failed: %s", cudaGetErrorString(e));
+    return PP_E_CUDA;
+  }
+  return PP_OK;
+}
+
+extern "C" int pp_msm_g1_bases_info(const pp_msm_bases *bases, uint64_t *n, uint32_t *window_bits,
+                                    uint64_t *table_bytes) {
+  if (!bases) {
+    pp::set_error("pp_msm_g1_bases_info: null handle");
+    return PP_E_INVAL;
+  }
+  const uint64_t W = 256 / bases->c + 1;
+  if (n) *n = bases->n;
+  if (window_bits) *window_bits = bases->c;
+  if (table_bytes) *table_bytes = W * bases->n * sizeof(pp::g1a);
+  return PP_OK;
+}
+
+extern "C" int pp_msm_g1_fixed(const pp_msm_bases *bases, const void *d_scalars, void *d_out,
+                               void *stream) {
+  using namespace pp;
+  auto aligned16 = [](const void *q) { return q && (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+  if (!bases || !aligned16(d_scalars) || !aligned16(d_out)) {
+    set_error("pp_msm_g1_fixed: need a handle and 16-byte aligned device buffers");
+    return PP_E_INVAL;
+  }
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != bases->device) {
+    set_error("pp_msm_g1_fixed: the tables live on device %d, the current device is %d",
+              bases->device, dev);
+    return PP_E_INVAL;
+  }
+  return msm_run(bases->table, static_cast<const uint32_t *>(d_scalars), bases->n,
+                 msm_plan_for(bases->c, 1), static_cast<fq *>(d_out), (cudaStream_t)stream);
+}
+
+// ---- s_i G for the generator: test and benchmark points, commitments to
+// known constants.  One thread per scalar, double-and-add from bit 255.
+namespace pp {
+namespace {
+
+__global__ void __launch_bounds__(kPointThreads)
+    k_g1_mul_gen(const uint32_t *__restrict__ scalars, uint64_t n, g1a *__restrict__ out) {
+  const g1a G = g1_generator();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t s[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s[k] = scalars[8 * i + k];
+    g1x acc = g1x_inf();
+    for (int b = 255; b >= 0; --b) {
+      acc = g1x_dbl(acc);
+      if ((s[b >> 5] >> (b & 31)) & 1u) acc = g1x_add_affine(acc, G);
+    }
+    out[i] = g1x_to_affine(acc);
+  }
+}
+
+}  // namespace
+}  // namespace pp
+
+extern "C" int pp_g1_mul_gen(const void *d_scalars, uint64_t n, void *d_out, void *stream) {
+  using namespace pp;
+  auto aligned16 = [](const void *q) { return q && (reinterpret_cast<uintptr_t>(q) & 15) == 0; };
+  if (n == 0) return PP_OK;
+  if (!aligned16(d_scalars) || !aligned16(d_out)) {
+    set_error("pp_g1_mul_gen: buffers must be 16-byte aligned device pointers");
+    return PP_E_INVAL;
+  }
+  k_g1_mul_gen<<<grid_for(n, kPointThreads, 16), kPointThreads, 0, (cudaStream_t)stream>>>(
+      static_cast<const uint32_t *>(d_scalars), n, static_cast<g1a *>(d_out));
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
 }
-
-extern "C" int pp_msm_g1_window_bits(uint64_t n) { return (int)pp::msm_plan(n).c; }

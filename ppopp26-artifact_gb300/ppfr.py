@@ -188,6 +188,72 @@ def msm_window_bits(n: int) -> int:
     return int(lib().pp_msm_g1_window_bits(n))
 
 
+def g1_mul_gen(scalars, out=None, stream=None):
+    """pp_g1_mul_gen: scalars (n, 4) int64 plain integers -> (n, 12) int64
+    affine points s_i G (all zero for infinity)."""
+    torch = _torch()
+    assert scalars.dim() == 2 and scalars.shape[1] == 4 and scalars.is_contiguous()
+    n = scalars.shape[0]
+    if out is None:
+        out = torch.empty((n, 12), dtype=torch.int64, device=scalars.device)
+    L = lib()
+    L.pp_g1_mul_gen.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    L.pp_g1_mul_gen.restype = ctypes.c_int
+    if n:
+        check(L.pp_g1_mul_gen(ctypes.c_void_p(scalars.data_ptr()), n, ctypes.c_void_p(out.data_ptr()),
+                              _stream(stream)))
+    return out
+
+
+class MsmBases:
+    """pp_msm_g1_bases_*: window tables of a fixed point set in HBM, for
+    repeated MSMs over the same points (pp_msm_g1_fixed).  Same results as
+    msm_g1 bit for bit."""
+
+    def __init__(self, points, window_bits: int = 0, stream=None):
+        L = lib()
+        if not hasattr(L, "_bases_proto"):
+            v = ctypes.c_void_p
+            L.pp_msm_g1_bases_create.argtypes = [v, ctypes.c_uint64, ctypes.c_uint32, v, v]
+            L.pp_msm_g1_bases_destroy.argtypes = [v]
+            L.pp_msm_g1_bases_info.argtypes = [v, v, v, v]
+            L.pp_msm_g1_fixed.argtypes = [v, v, v, v]
+            for f in (L.pp_msm_g1_bases_create, L.pp_msm_g1_bases_destroy, L.pp_msm_g1_bases_info,
+                      L.pp_msm_g1_fixed):
+                f.restype = ctypes.c_int
+            L._bases_proto = True
+        assert points.dim() == 2 and points.shape[1] == 12 and points.is_contiguous()
+        self.n = points.shape[0]
+        self._h = ctypes.c_void_p(0)
+        check(L.pp_msm_g1_bases_create(ctypes.c_void_p(points.data_ptr()), self.n, window_bits,
+                                       ctypes.byref(self._h), _stream(stream)))
+        n, c, nbytes = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(L.pp_msm_g1_bases_info(self._h, ctypes.byref(n), ctypes.byref(c), ctypes.byref(nbytes)))
+        self.window_bits, self.table_bytes = int(c.value), int(nbytes.value)
+        self._device = points.device
+
+    def msm(self, scalars, out=None, stream=None):
+        """sum_i s_i P_i -> (3, 6) int64 Jacobian point (x, y, 1), all zero for infinity."""
+        torch = _torch()
+        assert scalars.shape == (self.n, 4) and scalars.is_contiguous()
+        if out is None:
+            out = torch.empty((3, 6), dtype=torch.int64, device=self._device)
+        check(lib().pp_msm_g1_fixed(self._h, ctypes.c_void_p(scalars.data_ptr()),
+                                    ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def close(self):
+        if self._h:
+            check(lib().pp_msm_g1_bases_destroy(self._h))
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # -------------------------------------------------------------- data formats
 def read_raw(path: str, n: int = None, pinned: bool = True):
     """Raw file of 32-byte little-endian Montgomery elements (the reference's
