@@ -79,6 +79,8 @@ int pp_tune_load(const char *path);
  *    INTT, multiply coefficient i by 7^i, zero-pad, NTT: p(7 * w_L^k).
  *  mode 2 (PP_LDE_SPREAD): the reference's naive_lde baseline (lde.cu:1367,
  *    spread at :479-491): inputs placed at i << lambda, no coset factor.
+ *    That transform equals NTT_N(a)[k mod N]; it is computed as one
+ *    2^lg_n-point transform and 2^lambda - 1 copies.
  * d_out must not overlap d_in.  lambda <= 8. */
 #define PP_LDE_COEFFS 0
 #define PP_LDE_EVALS 1

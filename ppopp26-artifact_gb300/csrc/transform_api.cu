@@ -34,10 +34,22 @@ int lde_run(const fr *in, fr *out, uint32_t lg_n, uint32_t lambda, uint32_t mode
   desc.out_host = out_host;
   int st = PP_OK;
   if (mode == PP_LDE_SPREAD) {
-    desc.kind = pp::NTT_IN_SPREAD;
-    desc.spread = lambda;
-    desc.n_valid = 0;
-    return pp::ntt_run(in, out, L, false, desc, s);
+    // inputs at i << lambda, no coset factor: X_k = sum_i a_i w_L^(i 2^lambda k)
+    // = NTT_N(a)[k mod N] -- one N-point transform, then 2^lambda - 1 copies
+    // of it (the same values as the 2^L-point transform of the spread input)
+    const uint64_t n = 1ull << lg_n;
+    pp::NttInputDesc plain;
+    plain.in_host = in_host;
+    fr *first = out;
+    if (out_host) {
+      first = static_cast<fr *>(pp::workspace_get(sizeof(fr) << lg_n, s, 2, &st));
+      if (st) return st;
+    }
+    st = pp::ntt_run(in, first, lg_n, false, plain, s);
+    if (st) return st;
+    for (uint64_t r = out_host ? 0 : 1; r < (1ull << lambda); ++r)
+      PP_CUDA_TRY(cudaMemcpyAsync(out + r * n, first, sizeof(fr) * n, cudaMemcpyDefault, s));
+    return PP_OK;
   }
   if (mode == PP_LDE_COEFFS) {
     // coefficient i scaled by (7^(2^lambda))^i
