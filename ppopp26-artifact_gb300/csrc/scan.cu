@@ -23,6 +23,16 @@
 
 namespace pp {
 
+// Blocks per SM each operator's geometry aims for (scan_geom): longer chunks
+// cut the summaries to scan, more blocks hide more latency.  Swept over 1, 2,
+// 4, 8 and 16 on GB300 at 2^20 / 2^22 elements: grand product 2 (80.0 us
+// against 86.5 for 4; 4 is 3 % faster at 2^22), evaluation 2 (58 / 121
+// against 68 / 128), division 2 (94.5 / 222 against 128 / 252), permutation
+// product 8 (574 / 2125 against 592 / 2180; its local pass runs 2 blocks per
+// SM, so it needs more of them to hide latency).
+constexpr uint32_t kGpBlocksPerSm = 2, kEvalBlocksPerSm = 2, kDivBlocksPerSm = 2,
+                   kPermBlocksPerSm = 8;
+
 // ---------------------------------------------------------------- helpers
 // Block scans are work-efficient (Blelloch, "Prefix sums and their
 // applications", 1990): an up-sweep and a down-sweep over a balanced tree,
@@ -410,12 +420,14 @@ __global__ void __launch_bounds__(kScanThreads)
 // --------------------------------------------- backward affine recurrence
 // S_i = p_i + m * S_{i+1}: a thread's chunk [lo, hi) is the map
 // S_lo = L + m^(hi-lo) * S_hi with L its Horner value.
-__device__ __forceinline__ void chunk_map(const fr *p, uint64_t lo, uint64_t hi, const fr &m, fr &a,
-                                          fr &b) {
+// m_k = m^k for the full chunk length k, shared by the block: only a shorter
+// (last) chunk computes its own power.
+__device__ __forceinline__ void chunk_map(const fr *p, uint64_t lo, uint64_t hi, uint64_t k,
+                                          const fr &m, const fr &m_k, fr &a, fr &b) {
   fr L = fr_zero();
   for (uint64_t i = hi; i > lo; --i) L = fr_add(ld_fr(p + i - 1), fr_mul(m, L));
   a = L;
-  b = hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
+  b = hi - lo == k ? m_k : hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
 }
 
 // per-thread exclusive suffix map (optional) and per-block map
@@ -425,13 +437,16 @@ __global__ void __launch_bounds__(kScanThreads) k_affine_local(const fr *__restr
                                                                 fr *thread_b, fr *block_a,
                                                                 fr *block_b) {
   __shared__ fr sa[kScanThreads], sb[kScanThreads];
+  __shared__ fr s_mk;
   fr m = ld_fr(m_ptr);
   if (negate_m) m = fr_neg(m);
+  if (threadIdx.x == 0) s_mk = fr_pow_u64(m, g.k);
+  __syncthreads();
   const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
   const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
   fr a, b;
-  chunk_map(p, lo, hi, m, a, b);
+  chunk_map(p, lo, hi, g.k, m, s_mk, a, b);
   block_affine_suffix(a, b, sa, sb, thread_a != nullptr);
   if (thread_a && gt < g.threads) {
     const bool last = threadIdx.x == blockDim.x - 1;
@@ -511,7 +526,7 @@ extern "C" int pp_gp_scan(const void *d_in, void *d_excl, void *d_incl, uint64_t
     return PP_E_INVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const pp::ScanGeom g = pp::scan_geom(n);
+  const pp::ScanGeom g = pp::scan_geom(n, pp::kGpBlocksPerSm);
   int st = PP_OK;
   fr *ws = static_cast<fr *>(
       pp::workspace_get((g.threads + g.blocks) * sizeof(fr), s, 1, &st));
@@ -544,7 +559,7 @@ extern "C" int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *s
     return PP_E_INVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const pp::ScanGeom g = pp::scan_geom(n);
+  const pp::ScanGeom g = pp::scan_geom(n, pp::kDivBlocksPerSm);
   int st = PP_OK;
   fr *ws = static_cast<fr *>(
       pp::workspace_get((2 * g.threads + 2 * g.blocks) * sizeof(fr), s, 1, &st));
@@ -575,7 +590,7 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
     PP_LAUNCH_CHECK();
     return PP_OK;
   }
-  const pp::ScanGeom g = pp::scan_geom(n);
+  const pp::ScanGeom g = pp::scan_geom(n, pp::kEvalBlocksPerSm);
   int st = PP_OK;
   fr *ws = static_cast<fr *>(pp::workspace_get(2 * g.blocks * sizeof(fr), s, 1, &st));
   if (st) return st;
@@ -608,7 +623,7 @@ extern "C" int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, co
   }
   cudaStream_t s = (cudaStream_t)stream;
   const uint64_t n = 1ull << lg_n;
-  const pp::ScanGeom g = pp::scan_geom(n);
+  const pp::ScanGeom g = pp::scan_geom(n, pp::kPermBlocksPerSm);
   int st = PP_OK;
   const fr *omega_pow = pp::pow_table(pp::host_root_of_unity((int)lg_n, false), lg_n, &st);
   if (st) return st;

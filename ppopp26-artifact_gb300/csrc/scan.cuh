@@ -20,11 +20,12 @@ struct ScanGeom {
 
 int device_sm_count();
 
-// about four blocks of 256 threads per SM, at least 4 elements per thread
-inline ScanGeom scan_geom(uint64_t n) {
+// about blocks_per_sm blocks of 256 threads per SM, at least 4 elements per
+// thread (fewer blocks: longer chunks, fewer summaries to scan)
+inline ScanGeom scan_geom(uint64_t n, uint32_t blocks_per_sm = 4) {
   ScanGeom g;
   g.n = n;
-  const uint64_t target_threads = (uint64_t)device_sm_count() * 4 * kScanThreads;
+  const uint64_t target_threads = (uint64_t)device_sm_count() * blocks_per_sm * kScanThreads;
   uint64_t k = (n + target_threads - 1) / target_threads;
   if (k < 4) k = 4;
   g.k = k;
