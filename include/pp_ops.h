@@ -128,6 +128,34 @@ int pp_gp_scan(const void *d_in, void *d_excl, void *d_incl, uint64_t n, void *s
 int pp_gp_perm(const void *const *d_w, const void *const *d_sigma, const void *d_params, void *d_z,
                uint32_t lg_n, void *stream);
 
+/* ------------------------------------------------- element-wise Fr ops ---
+ * Vectors of n field elements (Montgomery form).  The output may be the
+ * same buffer as an input (the reference's in-place "_" forms).
+ * Replace add_mod / sub_mod / mul_mod / div_mod and their _ and _scalar
+ * forms, neg_mod, inv_mod, exp_mod, gen_sequence and repeat_to_poly
+ * (PLONK/utils/function.cu:23-170 -> PLONK/utils/mont/cuda/
+ * mont_arithmetic.cu:6-52, :414-520).
+ *
+ * pp_fr_binary: c[i] = a[i] op b[i], or a[i] op b[0] when b_is_scalar (b must
+ * then not overlap c).  Division by 0 gives 0, as the reference's
+ * reciprocal (ff/mont_t.cuh:1117) does.  pp_fr_unary: c[i] = -a[i] or
+ * 1 / a[i] (0 for 0).  pp_fr_pow: c[i] = a[i]^exponent for any exponent,
+ * 0 and 1 included (the reference's exp_mod traps for exponents below 2).
+ * pp_fr_powers: out[i] = x^i (gen_sequence).  pp_fr_fill: out[i] = x
+ * (repeat_to_poly).  x is one element that must not lie inside the output. */
+#define PP_FR_ADD 0
+#define PP_FR_SUB 1
+#define PP_FR_MUL 2
+#define PP_FR_DIV 3
+int pp_fr_binary(uint32_t op, const void *d_a, const void *d_b, void *d_c, uint64_t n,
+                 int b_is_scalar, void *stream);
+#define PP_FR_NEG 0
+#define PP_FR_INV 1
+int pp_fr_unary(uint32_t op, const void *d_a, void *d_c, uint64_t n, void *stream);
+int pp_fr_pow(const void *d_a, void *d_c, uint64_t n, uint64_t exponent, void *stream);
+int pp_fr_powers(const void *d_x, void *d_out, uint64_t n, void *stream);
+int pp_fr_fill(const void *d_x, void *d_out, uint64_t n, void *stream);
+
 /* --------------------------------------------------------- evaluation ---
  * d_y[0] = sum_i poly[i] * x^i (x = d_x[0]); n == 0 gives 0.
  * Replaces evaluate (PLONK/utils/function.cu:170-181 ->

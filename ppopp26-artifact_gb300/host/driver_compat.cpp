@@ -23,6 +23,9 @@
 //   pp_compat_driver convert <n> <in.bin> <outdir>
 //       read_file, to_base -> base.bin and base.txt (writeToFile), to_mont of
 //       that -> mont.bin (the input again)
+//   pp_compat_driver fieldops <n> <dir>
+//       add_mod ... make_tensor on <dir>/{a,b,s}.bin -> <dir>/<name>.bin, and
+//       gt_zkp of (a, b) and (b, a) on stdout
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -184,8 +187,46 @@ static int convert(size_t n, const std::string &in, const std::string &outdir) {
   return 0;
 }
 
+// element-wise operators and buffer helpers on a, b (n elements) and s (one)
+static int fieldops(size_t n, const std::string &dir) {
+  SyncedMemory a = load(dir + "/a.bin", n), b = load(dir + "/b.bin", n), s = load(dir + "/s.bin", 1);
+  struct Out {
+    const char *name;
+    SyncedMemory m;
+  };
+  std::vector<Out> outs;
+  outs.push_back({"add", add_mod(a, b)});
+  outs.push_back({"sub", sub_mod(a, b)});
+  outs.push_back({"mul", mul_mod(a, b)});
+  outs.push_back({"div", div_mod(a, b)});
+  SyncedMemory ip = load(dir + "/a.bin", n);
+  div_mod_(ip, b);
+  outs.push_back({"div_in_place", ip});
+  outs.push_back({"add_scalar", add_mod_scalar(a, s)});
+  outs.push_back({"div_scalar", div_mod_scalar(a, s)});
+  SyncedMemory ms = load(dir + "/a.bin", n);
+  mul_mod_scalar_(ms, s);
+  outs.push_back({"mul_scalar_in_place", ms});
+  outs.push_back({"neg", neg_mod(a)});
+  outs.push_back({"inv", inv_mod(b)});
+  outs.push_back({"exp5", exp_mod(a, 5)});
+  outs.push_back({"seq", gen_sequence(n, s)});
+  outs.push_back({"rep", repeat_to_poly(s, n)});
+  outs.push_back({"pad", pad_poly(a, 2 * n)});
+  outs.push_back({"cat", cat(a, b)});
+  outs.push_back({"slice", slice(a, n / 2, false)});
+  outs.push_back({"tensor", make_tensor(a, 4 * n)});
+  cudaDeviceSynchronize();
+  for (auto &o : outs) write_file(dir + "/" + o.name + ".bin", o.m.mutable_cpu_data(), o.m.size());
+  std::printf("gt %d %d\n", gt_zkp(a, b) ? 1 : 0, gt_zkp(b, a) ? 1 : 0);
+  std::printf("fieldops ok\n");
+  return 0;
+}
+
 int main(int argc, char **argv) {
   try {
+    if (argc >= 4 && std::string(argv[1]) == "fieldops")
+      return fieldops(std::strtoull(argv[2], nullptr, 10), argv[3]);
     if (argc >= 5 && std::string(argv[1]) == "miss_ops") return miss_ops(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 5 && std::string(argv[1]) == "ntt") return ntt_check(std::atoi(argv[2]), argv[3], argv[4]);
     if (argc >= 4 && std::string(argv[1]) == "quotient")
@@ -203,6 +244,6 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "error (status %d): %s\n", e.status(), e.what());
     return 3;
   }
-  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate|convert|msm ...\n", argv[0]);
+  std::fprintf(stderr, "usage: %s miss_ops|ntt|lde|quotient|gate|convert|msm|fieldops ...\n", argv[0]);
   return 1;
 }

@@ -43,6 +43,52 @@ void accumulate_mul_poly_(SyncedMemory product, SyncedMemory output,
 SyncedMemory evaluate(SyncedMemory poly, SyncedMemory x);
 SyncedMemory poly_div_poly(SyncedMemory divid, SyncedMemory c);
 
+// ---- element-wise field operators and buffer helpers
+// (PLONK/utils/function.cuh:12-71, zk_function.cu:3), in field_ops.cpp.  The
+// arithmetic runs on the GPU whatever the head of the inputs (the reference
+// has CPU twins for some of them; the values are the same).  The inverse of
+// 0 is 0.  exp_mod takes any exponent >= 0 (the reference traps below 2) and
+// throws for a negative one.
+SyncedMemory neg_mod(SyncedMemory input);
+SyncedMemory inv_mod(SyncedMemory input);
+SyncedMemory add_mod(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+void add_mod_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory sub_mod(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+void sub_mod_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory mul_mod(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+void mul_mod_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory div_mod(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+void div_mod_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory exp_mod(SyncedMemory input, int exp);
+SyncedMemory add_mod_scalar(SyncedMemory input1, SyncedMemory input2,
+                            cudaStream_t stream = (cudaStream_t)0);
+void add_mod_scalar_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory sub_mod_scalar(SyncedMemory input1, SyncedMemory input2,
+                            cudaStream_t stream = (cudaStream_t)0);
+void sub_mod_scalar_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory mul_mod_scalar(SyncedMemory input1, SyncedMemory input2,
+                            cudaStream_t stream = (cudaStream_t)0);
+void mul_mod_scalar_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory div_mod_scalar(SyncedMemory input1, SyncedMemory input2,
+                            cudaStream_t stream = (cudaStream_t)0);
+void div_mod_scalar_(SyncedMemory input1, SyncedMemory input2, cudaStream_t stream = (cudaStream_t)0);
+// [1, x, x^2, ..., x^(N-1)]
+SyncedMemory gen_sequence(uint64_t N, SyncedMemory x, cudaStream_t stream = (cudaStream_t)0);
+void gen_sequence_(uint64_t N, SyncedMemory x, SyncedMemory y, cudaStream_t stream = (cudaStream_t)0);
+// N copies of x[0]
+SyncedMemory repeat_to_poly(SyncedMemory x, uint64_t N, cudaStream_t stream = (cudaStream_t)0);
+void repeat_to_poly_(SyncedMemory x, SyncedMemory y, uint64_t N, cudaStream_t stream = (cudaStream_t)0);
+// x followed by zeros up to N elements (x must not be longer)
+SyncedMemory pad_poly(SyncedMemory x, uint64_t N, cudaStream_t stream = (cudaStream_t)0);
+void pad_poly_(SyncedMemory x, SyncedMemory out, uint64_t N, cudaStream_t stream = (cudaStream_t)0);
+SyncedMemory repeat_zero(uint64_t N);  // N zero elements in host memory
+SyncedMemory cat(SyncedMemory a, SyncedMemory b);
+SyncedMemory slice(SyncedMemory a, uint64_t len, bool forward);  // first / last len elements
+// pad_len elements; element i holds the 64-bit word i of input as (w, 0, 0, 0)
+SyncedMemory make_tensor(SyncedMemory input, uint64_t pad_len);
+// a > b as integers of little-endian 64-bit words (host data)
+bool gt_zkp(SyncedMemory a, SyncedMemory b);
+
 class Ntt {
  public:
   // The reference's twiddle blob; the transform tables here are cached by

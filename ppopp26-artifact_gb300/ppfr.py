@@ -184,6 +184,75 @@ def msm_g1(points, scalars, out=None, stream=None):
     return out
 
 
+FR_ADD, FR_SUB, FR_MUL, FR_DIV = 0, 1, 2, 3
+FR_NEG, FR_INV = 0, 1
+
+
+def _ew_proto(L):
+    if not hasattr(L, "_ew_proto"):
+        v, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+        for name, args in (("pp_fr_binary", [u32, v, v, v, u64, ctypes.c_int, v]),
+                           ("pp_fr_unary", [u32, v, v, u64, v]), ("pp_fr_pow", [v, v, u64, u64, v]),
+                           ("pp_fr_powers", [v, v, u64, v]), ("pp_fr_fill", [v, v, u64, v])):
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._ew_proto = True
+    return L
+
+
+def fr_binary(op: int, a, b, out=None, stream=None):
+    """pp_fr_binary: a op b element-wise, or a op b[0] when b has one element
+    (the reference's *_mod_scalar).  out may be a or b (the in-place forms)."""
+    n = a.shape[0]
+    scalar = b.shape[0] == 1 and n != 1
+    assert scalar or b.shape[0] == n
+    if out is None:
+        out = empty(n, a.device)
+    L = _ew_proto(lib())
+    check(L.pp_fr_binary(op, _ptr(a) if n else None, _ptr(b), _ptr(out) if n else None, n, int(scalar),
+                         _stream(stream)))
+    return out
+
+
+def fr_unary(op: int, a, out=None, stream=None):
+    """pp_fr_unary: -a or 1 / a (0 for 0) element-wise."""
+    n = a.shape[0]
+    if out is None:
+        out = empty(n, a.device)
+    if n:
+        check(_ew_proto(lib()).pp_fr_unary(op, _ptr(a), _ptr(out), n, _stream(stream)))
+    return out
+
+
+def fr_pow(a, exponent: int, out=None, stream=None):
+    """pp_fr_pow: a^exponent element-wise (exponent < 2^64)."""
+    n = a.shape[0]
+    if out is None:
+        out = empty(n, a.device)
+    if n:
+        check(_ew_proto(lib()).pp_fr_pow(_ptr(a), _ptr(out), n, exponent, _stream(stream)))
+    return out
+
+
+def fr_powers(x, n: int, out=None, stream=None):
+    """pp_fr_powers (gen_sequence): [1, x, x^2, ..., x^(n-1)]."""
+    if out is None:
+        out = empty(n, x.device)
+    if n:
+        check(_ew_proto(lib()).pp_fr_powers(_ptr(x), _ptr(out), n, _stream(stream)))
+    return out
+
+
+def fr_fill(x, n: int, out=None, stream=None):
+    """pp_fr_fill (repeat_to_poly): n copies of x."""
+    if out is None:
+        out = empty(n, x.device)
+    if n:
+        check(_ew_proto(lib()).pp_fr_fill(_ptr(x), _ptr(out), n, _stream(stream)))
+    return out
+
+
 def msm_window_bits(n: int) -> int:
     return int(lib().pp_msm_g1_window_bits(n))
 

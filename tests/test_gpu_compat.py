@@ -110,3 +110,41 @@ def test_msm_driver_matches_blst(pp, cuda, tmp_path, case):
     run("msm", len(pts), tmp_path / "p.bin", tmp_path / "s.bin", tmp_path / "o.bin")
     o = np.fromfile(tmp_path / "o.bin", dtype=np.uint64).reshape(3, 6)
     assert np.array_equal(np.concatenate([o[0], o[1]]), g[case + "/out"])
+
+
+@pytest.mark.parametrize("n", [2, 64, 1000])
+def test_fieldops_driver(pp, O, cuda, tmp_path, n):
+    """add_mod ... make_tensor and gt_zkp through the C++ layer."""
+    a = O.random_fr(n, 0x5100 + n)
+    b = O.random_fr(n, 0x5200 + n)
+    b[1] = 0  # division by 0 gives 0
+    s = O.random_fr(1, 0x5300 + n)
+    a.tofile(tmp_path / "a.bin")
+    b.tofile(tmp_path / "b.bin")
+    s.tofile(tmp_path / "s.bin")
+    out = run("fieldops", n, tmp_path)
+    gt_ab = [int(t) for t in out.split("gt ")[1].split()[:2]]
+    big = lambda x: sum(int(w) << (64 * k) for k, w in enumerate(x.ravel()))  # noqa: E731
+    assert gt_ab == [int(big(a) > big(b)), int(big(b) > big(a))]
+    f = lambda name, m=n: load(tmp_path / (name + ".bin"), m)  # noqa: E731
+    inv = lambda y: O.fr_inv(y)  # noqa: E731  (inverse of 0 is 0)
+    for i in range(n):
+        assert (f("add")[i] == O.fr_add(a[i], b[i])).all()
+        assert (f("sub")[i] == O.fr_sub(a[i], b[i])).all()
+        assert (f("mul")[i] == O.fr_mul(a[i], b[i])).all()
+        q = O.fr_mul(a[i], inv(b[i]))
+        assert (f("div")[i] == q).all() and (f("div_in_place")[i] == q).all()
+        assert (f("add_scalar")[i] == O.fr_add(a[i], s[0])).all()
+        assert (f("div_scalar")[i] == O.fr_mul(a[i], inv(s[0]))).all()
+        assert (f("mul_scalar_in_place")[i] == O.fr_mul(a[i], s[0])).all()
+        assert (f("neg")[i] == O.fr_neg(a[i])).all()
+        assert (f("inv")[i] == inv(b[i])).all()
+        assert (f("exp5")[i] == O.fr_pow(a[i], 5)).all()
+        assert (f("seq")[i] == O.fr_pow(s[0], i)).all()
+        assert (f("rep")[i] == s[0]).all()
+    pad = f("pad", 2 * n)
+    assert (pad[:n] == a).all() and not pad[n:].any()
+    assert (f("cat", 2 * n) == np.concatenate([a, b])).all()
+    assert (f("slice", n // 2) == a[n - n // 2:]).all()
+    tensor = f("tensor", 4 * n)
+    assert (tensor[:, 0] == a.ravel()).all() and not tensor[:, 1:].any()
