@@ -429,11 +429,33 @@ def secondary_ops(pp, torch):
     zz = ppfr.empty(n)
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
     del w, s, p
+    elementwise_bench(pp, torch, rate, res)
     constraint_bench(pp, torch, rate, res)
     msm_bench(pp, torch, rate, res)
     res["batched"] = batched_bench(pp, torch)
     res["serving"] = serving_bench(pp, torch)
     return res
+
+
+def elementwise_bench(pp, torch, rate, res):
+    """Element-wise operators over 2^24 elements (512 MiB per vector, larger
+    than L2), with their HBM fraction: mul_mod reads two vectors and writes
+    one (96 B per element), div_mod the same plus 3 multiplies and 1/32 of an
+    inversion per element, gen_sequence writes one (32 B per element)."""
+    ppfr = pp.ppfr
+    n = N
+    a, b = pp.random_fr(n, 40), pp.random_fr(n, 41)
+    c = ppfr.empty(n)
+    x = pp.random_fr(1, 42)
+    peaks, _ = load_peaks()
+    for name, fn, nbytes in (("mul_mod_2^24", lambda: ppfr.fr_binary(ppfr.FR_MUL, a, b, out=c), 96),
+                             ("add_mod_2^24", lambda: ppfr.fr_binary(ppfr.FR_ADD, a, b, out=c), 96),
+                             ("div_mod_2^24", lambda: ppfr.fr_binary(ppfr.FR_DIV, a, b, out=c), 96),
+                             ("gen_sequence_2^24", lambda: ppfr.fr_powers(x, n, out=c), 32)):
+        rate(name, fn, n, 5)
+        gbs = nbytes * n / (res[name]["ms"] / 1e3) / 1e9
+        res[name].update({"GB_per_s": round(gbs, 1), "hbm_frac": round(gbs / peaks["hbm_gbs"], 3)})
+    del a, b, c
 
 
 def constraint_bench(pp, torch, rate, res):

