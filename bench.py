@@ -487,12 +487,35 @@ def constraint_bench(pp, torch, rate, res):
     del w, sig, x, z, zn, mod, l1
     V = {k: vec(20 + i) for i, k in enumerate(ppfr.GATE_VECTORS)}
     S = {k: scal(20 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
-    name = "gate_constraint_2^22"
+    # the prover's constants (one .. eightythree as integers): 81 multiplies
+    # per point; any other scalars: 104
+    name = "gate_constraint_2^22_general_scalars"
     rate(name, lambda: ppfr.gate_constraint(V, S, 5, out=out), n, 3)
     res[name].update({"MM_per_point": 104, "bytes_per_point": 736})
-    for k, mm in (("quotient_permutation_2^22", 18), ("gate_constraint_2^22", 104)):
+    S.update(gate_small_constants(ppfr))
+    name = "gate_constraint_2^22"
+    rate(name, lambda: ppfr.gate_constraint(V, S, 5, out=out), n, 3)
+    res[name].update({"MM_per_point": 81, "bytes_per_point": 736})
+    for k in ("quotient_permutation_2^22", "gate_constraint_2^22",
+              "gate_constraint_2^22_general_scalars"):
         pts = res[k]["Melem_per_s"] * 1e6
+        mm = res[k]["MM_per_point"]
         res[k]["int_frac_of_nominal_peak"] = round(pts * mm * 256 / peak, 4)
+
+
+def gate_small_constants(ppfr):
+    """four, one, two, three, nine, eighteen, eightyone, eightythree as the
+    prover passes them: Montgomery forms of those integers, made on the
+    device as powers of one plus additions."""
+    one = ppfr.fr_powers(ppfr.random_fr(1, 0xE0), 1)  # x^0 = one
+    out = {"one": one}
+    for k, v in (("two", 2), ("three", 3), ("four", 4), ("nine", 9), ("eighteen", 18),
+                 ("eightyone", 81), ("eightythree", 83)):
+        acc = one
+        for _ in range(v - 1):
+            acc = ppfr.fr_binary(ppfr.FR_ADD, acc, one)
+        out[k] = acc
+    return out
 
 
 def profile_op(args, pp, torch):
@@ -516,6 +539,7 @@ def profile_op(args, pp, torch):
     elif args.op == "gate":
         V = {k: ppfr.random_fr(n, 0x20 + i) for i, k in enumerate(ppfr.GATE_VECTORS)}
         S = {k: ppfr.random_fr(1, 0x80 + i) for i, k in enumerate(ppfr.GATE_SCALARS)}
+        S.update(gate_small_constants(ppfr))
         out = ppfr.empty(n)
         fn = lambda: ppfr.gate_constraint(V, S, 5, out=out)  # noqa: E731
     elif args.op == "gpperm":

@@ -96,57 +96,107 @@ __device__ __forceinline__ fr delta4(const fr &x, const fr &k312) {
   return fr_mul(fr_mul(x2, x2), k312);
 }
 
+// small multiples by additions (exact, like any field identity)
+__device__ __forceinline__ fr dbl(const fr &x) { return fr_add(x, x); }
+__device__ __forceinline__ fr mul3(const fr &x) { return fr_add(dbl(x), x); }
+__device__ __forceinline__ fr mul4(const fr &x) { return dbl(dbl(x)); }
+__device__ __forceinline__ fr mul6(const fr &x) { return dbl(mul3(x)); }
+__device__ __forceinline__ fr mul9(const fr &x) { return fr_add(dbl(mul4(x)), x); }
+__device__ __forceinline__ fr mul18(const fr &x) { return dbl(mul9(x)); }
+__device__ __forceinline__ fr mul36(const fr &x) { return dbl(mul18(x)); }
+__device__ __forceinline__ fr mul81(const fr &x) { return mul9(mul9(x)); }
+__device__ __forceinline__ fr mul83(const fr &x) { return fr_add(mul81(x), dbl(x)); }
+
+// 6 x^4 (delta4 with three one two = 6)
+__device__ __forceinline__ fr delta4_6(const fr &x) {
+  const fr x2 = fr_mul(x, x);
+  return mul6(fr_mul(x2, x2));
+}
+
 // The gate runs as three launches so that each keeps its live values in
 // fewer registers (more resident warps): the range and logic terms are
 // written first, then the arithmetic and public-input terms and the fixed-
 // and variable-base group additions are added.
-__device__ __forceinline__ void stage_scalars(const GateArgs &a, fr *sc) {
+
+// Stages the scalars (and three one two) in shared memory and returns whether
+// four, one, two, three, nine, eighteen, eightyone and eightythree hold those
+// integers, as the prover passes them.  Then the kernels take SMALL = true:
+// multiplies by them become additions and one one / three one two drop out,
+// with the same field values (2^22 points: range and logic 47 -> 27
+// multiplies per point, groups 38 -> 35).  Any other values take SMALL =
+// false, the expression as written.  Every thread gets the same answer.
+__device__ __forceinline__ bool stage_scalars(const GateArgs &a, fr *sc) {
+  __shared__ int s_small;
   if (threadIdx.x < PP_GATE_NS) sc[threadIdx.x] = ldg_fr(a.s[threadIdx.x]);
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     sc[PP_GATE_NS] =
         fr_mul(fr_mul(sc[PP_GATE_S_THREE], sc[PP_GATE_S_ONE]), sc[PP_GATE_S_TWO]);
+    const fr one = fr_one();
+    s_small = fr_eq(sc[PP_GATE_S_ONE], one) && fr_eq(sc[PP_GATE_S_TWO], dbl(one)) &&
+              fr_eq(sc[PP_GATE_S_THREE], mul3(one)) && fr_eq(sc[PP_GATE_S_FOUR], mul4(one)) &&
+              fr_eq(sc[PP_GATE_S_NINE], mul9(one)) && fr_eq(sc[PP_GATE_S_EIGHTEEN], mul18(one)) &&
+              fr_eq(sc[PP_GATE_S_EIGHTYONE], mul81(one)) &&
+              fr_eq(sc[PP_GATE_S_EIGHTYTHREE], mul83(one));
+  }
   __syncthreads();
+  return s_small != 0;
 }
 
 #define S(name) sc[PP_GATE_S_##name]
 #define V(name) ldcs_fr(a.v[PP_GATE_V_##name] + i)
 
+// The host launches both forms; the one whose SMALL does not match the
+// scalars returns after staging them.
+template <bool SMALL>
 __global__ void __launch_bounds__(kThreads, 2) k_gate_range_logic(const GateArgs a, fr *out,
                                                                uint64_t n) {
   __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
-  stage_scalars(a, sc);
+  if (stage_scalars(a, sc) != SMALL) return;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const fr k312 = sc[PP_GATE_NS];
     const fr a_ = V(A), b = V(B), c = V(C), d = V(D), dn = V(D_NEXT);
-    const fr four = S(FOUR);
-    const fr a4 = fr_mul(a_, four), b4 = fr_mul(b, four), c4 = fr_mul(c, four),
-             d4 = fr_mul(d, four);
+    fr a4, b4, c4, d4;
+    if constexpr (SMALL) {
+      a4 = mul4(a_), b4 = mul4(b), c4 = mul4(c), d4 = mul4(d);
+    } else {
+      const fr four = S(FOUR);
+      a4 = fr_mul(a_, four), b4 = fr_mul(b, four), c4 = fr_mul(c, four), d4 = fr_mul(d, four);
+    }
+    auto quad = [&](const fr &x) { return SMALL ? delta4_6(x) : delta4(x, k312); };
 
     // range gate: four 2-bit quads
-    fr t = fr_mul(delta4(fr_sub(a4, dn), k312), S(KAPPA_CU_RANGE));
-    t = fr_add(t, fr_mul(delta4(fr_sub(a_, b4), k312), S(KAPPA_SQ_RANGE)));
-    t = fr_add(t, delta4(fr_sub(c, d4), k312));
-    t = fr_add(t, fr_mul(delta4(fr_sub(b, c4), k312), S(KAPPA_RANGE)));
+    fr t = fr_mul(quad(fr_sub(a4, dn)), S(KAPPA_CU_RANGE));
+    t = fr_add(t, fr_mul(quad(fr_sub(a_, b4)), S(KAPPA_SQ_RANGE)));
+    t = fr_add(t, quad(fr_sub(c, d4)));
+    t = fr_add(t, fr_mul(quad(fr_sub(b, c4)), S(KAPPA_RANGE)));
     fr acc = fr_mul(fr_mul(t, S(RANGE_CHALLENGE)), V(RANGE));
 
     // logic gate
     const fr da = fr_sub(a4, V(A_NEXT)), db = fr_sub(b4, V(B_NEXT));
     const fr w = fr_add(da, db), e = fr_sub(dn, d4);
     const fr da2 = fr_mul(da, da);
-    const fr inner =
-        fr_sub(fr_mul(w, S(EIGHTYONE)),
-               fr_add(fr_mul(c, fr_mul(fr_sub(c4, fr_mul(w, S(EIGHTEEN))), S(EIGHTYONE))),
-                      fr_mul(fr_add(da2, da2), S(EIGHTEEN))));
-    const fr A = fr_sub(fr_mul(fr_add(e, w), S(THREE)),
-                        fr_mul(fr_mul(c, fr_mul(inner, S(EIGHTYTHREE))), S(TWO)));
-    const fr B = fr_mul(V(Q_C), fr_sub(fr_mul(e, S(NINE)), fr_mul(w, S(THREE))));
+    fr inner, A, B, da4;
+    if constexpr (SMALL) {
+      inner = fr_sub(mul81(w), fr_add(fr_mul(c, mul81(fr_sub(c4, mul18(w)))), mul36(da2)));
+      A = fr_sub(mul3(fr_add(e, w)), dbl(fr_mul(c, mul83(inner))));
+      B = fr_mul(V(Q_C), fr_sub(mul9(e), mul3(w)));
+      da4 = mul6(fr_mul(da2, da2));
+    } else {
+      inner = fr_sub(fr_mul(w, S(EIGHTYONE)),
+                     fr_add(fr_mul(c, fr_mul(fr_sub(c4, fr_mul(w, S(EIGHTEEN))), S(EIGHTYONE))),
+                            fr_mul(fr_add(da2, da2), S(EIGHTEEN))));
+      A = fr_sub(fr_mul(fr_add(e, w), S(THREE)),
+                 fr_mul(fr_mul(c, fr_mul(inner, S(EIGHTYTHREE))), S(TWO)));
+      B = fr_mul(V(Q_C), fr_sub(fr_mul(e, S(NINE)), fr_mul(w, S(THREE))));
+      da4 = fr_mul(fr_mul(da2, da2), k312);
+    }
     fr l = fr_mul(fr_add(A, B), S(KAPPA_QU_LOGIC));
     l = fr_add(l, fr_mul(fr_sub(c, fr_mul(da, db)), S(KAPPA_CU_LOGIC)));
-    l = fr_add(l, delta4(e, k312));
-    l = fr_add(l, fr_mul(fr_mul(da2, da2), k312));
-    l = fr_add(l, delta4(db, k312));
+    l = fr_add(l, quad(e));
+    l = fr_add(l, da4);
+    l = fr_add(l, quad(db));
     acc = fr_add(acc, fr_mul(fr_mul(l, S(LOGIC_CHALLENGE)), V(LOGIC)));
     st_fr(out + i, acc);
   }
@@ -171,9 +221,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_gate_arith(const GateArgs a, fr
   }
 }
 
+template <bool SMALL>
 __global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a, fr *out, uint64_t n) {
   __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
-  stage_scalars(a, sc);
+  if (stage_scalars(a, sc) != SMALL) return;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const fr a_ = V(A), b = V(B), c = V(C), d = V(D);
@@ -183,17 +234,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a, f
     // fixed-base group addition
     fr f;
     {
-      const fr one = S(ONE);
       const fr abc = fr_mul(a_, bc);
-      const fr one2 = fr_mul(one, one);
       const fr dn2 = fr_mul(dn, dn);
-      const fr qr2 = fr_mul(fr_mul(V(Q_R), dn2), one2);
+      // one one = 1 when SMALL
+      const fr one2 = SMALL ? fr_one() : fr_mul(S(ONE), S(ONE));
+      const fr qr2 = SMALL ? fr_mul(V(Q_R), dn2) : fr_mul(fr_mul(V(Q_R), dn2), one2);
       const fr qldn = fr_mul(V(Q_L), dn);
       f = fr_mul(fr_sub(c, fr_mul(V(Q_C), dn)), S(KAPPA_FB));
       f = fr_add(f, fr_mul(fr_sub(fr_sub(bn, fr_mul(fr_mul(abc, bn), pd)),
                                   fr_sub(fr_mul(b, qr2), fr_mul(a_, fr_mul(qldn, S(P_A))))),
                            S(KAPPA_CU_FB)));
-      f = fr_add(f, fr_mul(fr_mul(dn2, dn), one2));
+      f = fr_add(f, SMALL ? fr_mul(dn2, dn) : fr_mul(fr_mul(dn2, dn), one2));
       f = fr_add(f, fr_mul(fr_sub(fr_add(an, fr_mul(fr_mul(abc, an), pd)),
                                   fr_add(fr_mul(b, qldn), fr_mul(a_, qr2))),
                            S(KAPPA_SQ_FB)));
@@ -324,7 +375,12 @@ extern "C" int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n
   }
   g.sbox_alpha = (uint32_t)a->sbox_alpha;
   const unsigned grid = pp::grid_for(n);
-  pp::k_gate_range_logic<<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+  // each pair: the form that does not match the scalars returns at once
+  pp::k_gate_range_logic<true><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+      g, static_cast<pp::fr *>(d_out), n);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gate_range_logic<false><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
       g, static_cast<pp::fr *>(d_out), n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
@@ -332,7 +388,11 @@ extern "C" int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n
       g, static_cast<pp::fr *>(d_out), n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gate_groups<<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+  pp::k_gate_groups<true><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
+      g, static_cast<pp::fr *>(d_out), n);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gate_groups<false><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
       g, static_cast<pp::fr *>(d_out), n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();

@@ -105,6 +105,24 @@ def test_gate_matches_oracle(pp, O, cuda, n, alpha):
     assert O.first_diff(out, O.gate_constraint(V, S, alpha)) == -1
 
 
+SMALL = {"one": 1, "two": 2, "three": 3, "four": 4, "nine": 9, "eighteen": 18,
+         "eightyone": 81, "eightythree": 83}
+
+
+@pytest.mark.parametrize("n,off", [(1, None), (4097, None), ((1 << 15) + 3, None),
+                                   (513, "one"), (513, "eightythree"), (513, "four")])
+def test_gate_small_constants(pp, O, cuda, n, off):
+    """The prover's natural constants (additions instead of multiplies) and
+    the same with one of them off by one (the general form): both bit-exact."""
+    P = pp.ppfr
+    V = {k: O.random_fr(n, 0x7A7E + i) for i, k in enumerate(P.GATE_VECTORS)}
+    S = {k: O.random_fr(1, 0x7CA1 + i)[0] for i, k in enumerate(P.GATE_SCALARS)}
+    for k, v in SMALL.items():
+        S[k] = O.mont(v + (k == off))
+    out = gate_run(P, V, S, 5)
+    assert O.first_diff(out, O.gate_constraint(V, S, 5)) == -1
+
+
 def test_edge_cases_and_errors(pp, O, cuda):
     import torch
     P = pp.ppfr
