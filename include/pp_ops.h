@@ -105,6 +105,21 @@ int pp_ntt_host(const void *h_in, void *h_out, uint32_t lg_n, int inverse, void 
 int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda, uint32_t mode,
                 void *stream);
 
+/* count transforms of page-locked host polynomials of 2^lg_n elements:
+ * h_out[j] = NTT (or INTT) of h_in[j].  h_in[j] == h_out[j] is allowed; an
+ * output must not overlap another polynomial's input.  Each polynomial is
+ * copied to HBM, transformed and copied back, and the copies of neighbouring
+ * polynomials overlap the transforms (two internal copy streams, three
+ * rotating device buffers of 32 * 2^lg_n bytes held as workspace of the
+ * stream).  Asynchronous on the stream: synchronise it before reading
+ * h_out.  Buffers that are not page-locked are refused with PP_E_INVAL
+ * before any copy is queued; count = 0 does nothing.  The reference's
+ * our_ntt (ntt.cu:979-1037) transforms one host polynomial per call and
+ * leaves overlap across polynomials to the caller; this is that loop with
+ * the overlap built in. */
+int pp_ntt_host_many(const void *const *h_in, void *const *h_out, uint32_t count, uint32_t lg_n,
+                     int inverse, void *stream);
+
 /* ------------------------------------------------------- grand product ---
  * Exclusive prefix product in place: out[0] = 1, out[i] = prod_{j<i} in[j].
  * Replaces accumulate_mul_poly (PLONK/utils/function.cu:256 ->

@@ -165,3 +165,104 @@ extern "C" int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_
   return lde_run(static_cast<const fr *>(din), static_cast<fr *>(const_cast<void *>(dout)), lg_n,
                  lambda, mode, (cudaStream_t)stream, true, true);
 }
+
+// ------------------------------------------- many host-resident polynomials
+// Each polynomial is copied to HBM by a copy engine, transformed there and
+// copied back, with the copies of neighbouring polynomials overlapping the
+// transforms: host-to-device copies on one internal stream, the transforms
+// on the caller's stream, device-to-host copies on another.  Three rotating
+// device buffers keep the transform the bound: a buffer is held for one
+// polynomial's two copies and its transform (about 9.6 ms at 2^24 over a
+// 200 GB/s host link), under three transforms of 4.3 ms.  The buffers are
+// workspace slots 5-7 of the caller's stream, and the call ends by making
+// the caller's stream wait for the last copy, so later work on that stream
+// (and a workspace reallocation, which synchronises it) is ordered after
+// every copy.
+extern "C" int pp_ntt_host_many(const void *const *h_in, void *const *h_out, uint32_t count,
+                                uint32_t lg_n, int inverse, void *stream) {
+  if (lg_n > PP_MAX_LG_N) {
+    pp::set_error("pp_ntt_host_many: lg_n = %u exceeds %d", lg_n, PP_MAX_LG_N);
+    return PP_E_UNSUPPORTED;
+  }
+  if (count == 0) return PP_OK;
+  if (!h_in || !h_out) {
+    pp::set_error("pp_ntt_host_many: the input and output pointer arrays are required");
+    return PP_E_INVAL;
+  }
+  const void *dev = nullptr;
+  for (uint32_t j = 0; j < count; ++j) {
+    int st = host_view(h_in[j], "pp_ntt_host_many", "an input", &dev);
+    if (!st) st = host_view(h_out[j], "pp_ntt_host_many", "an output", &dev);
+    if (st) return st;
+  }
+  constexpr int kBufs = 3;
+  const cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = sizeof(fr) << lg_n;
+  fr *buf[kBufs];
+  for (int b = 0; b < kBufs; ++b) {
+    int st = PP_OK;
+    buf[b] = static_cast<fr *>(pp::workspace_get(bytes, s, 5 + b, &st));
+    if (st) return st;
+  }
+  int st = pp::ntt_prepare(lg_n, inverse != 0);
+  if (st) return st;
+  // streams and events of this call; destroying them with work still queued
+  // is allowed (their resources go once that work completes)
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_in[kBufs] = {}, ev_cmp[kBufs] = {}, ev_out[kBufs] = {};
+  auto cleanup = [&]() {
+    if (s_in) cudaStreamDestroy(s_in);
+    if (s_out) cudaStreamDestroy(s_out);
+    if (ev_start) cudaEventDestroy(ev_start);
+    for (int b = 0; b < kBufs; ++b) {
+      if (ev_in[b]) cudaEventDestroy(ev_in[b]);
+      if (ev_cmp[b]) cudaEventDestroy(ev_cmp[b]);
+      if (ev_out[b]) cudaEventDestroy(ev_out[b]);
+    }
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming);
+  for (int b = 0; b < kBufs && e == cudaSuccess; ++b) {
+    e = cudaEventCreateWithFlags(&ev_in[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_cmp[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_out[b], cudaEventDisableTiming);
+  }
+  // the copy streams start after the work already queued on the caller's stream
+  if (e == cudaSuccess) e = cudaEventRecord(ev_start, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s_in, ev_start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s_out, ev_start, 0);
+  pp::NttInputDesc desc;
+  for (uint32_t j = 0; j < count && e == cudaSuccess && st == PP_OK; ++j) {
+    const int b = (int)(j % kBufs);
+    if (j >= (uint32_t)kBufs) e = cudaStreamWaitEvent(s_in, ev_out[b], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf[b], h_in[j], bytes, cudaMemcpyHostToDevice, s_in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_in[b], s_in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_in[b], 0);
+    if (e != cudaSuccess) break;
+    st = pp::ntt_run(buf[b], buf[b], lg_n, inverse != 0, desc, s);
+    if (st) break;
+    e = cudaEventRecord(ev_cmp[b], s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s_out, ev_cmp[b], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_out[j], buf[b], bytes, cudaMemcpyDeviceToHost, s_out);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_out[b], s_out);
+  }
+  // the caller's stream waits for the last device-to-host copy (the copies
+  // run in order on one stream, so that one covers them all)
+  cudaError_t e2 = cudaSuccess;
+  if (ev_start) {
+    cudaEvent_t done = nullptr;
+    e2 = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    if (e2 == cudaSuccess && s_out) e2 = cudaEventRecord(done, s_out);
+    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, done, 0);
+    if (done) cudaEventDestroy(done);
+  }
+  cleanup();
+  if (st) return st;
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    pp::set_error("pp_ntt_host_many: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    cudaGetLastError();
+    return PP_E_CUDA;
+  }
+  return PP_OK;
+}

@@ -42,6 +42,7 @@ def lib():
                 "pp_ntt": [v, v, u32, i, v],
                 "pp_lde": [v, v, u32, u32, u32, v],
                 "pp_ntt_host": [v, v, u32, i, v],
+                "pp_ntt_host_many": [v, v, u32, u32, i, v],
                 "pp_to_mont": [v, v, u64, v],
                 "pp_msm_g1": [v, v, u64, v, v],
                 "pp_msm_g1_window_bits": [u64],
@@ -157,6 +158,23 @@ def ntt_host(x, inverse: bool = False, out=None, stream=None):
         out = empty_pinned(x.shape[0])
     check(lib().pp_ntt_host(_hptr(x), _hptr(out), lg, int(inverse), _stream(stream)))
     return out
+
+
+def ntt_host_many(xs, inverse: bool = False, outs=None, stream=None):
+    """pp_ntt_host_many: transforms of equal-sized page-locked host tensors,
+    copies of neighbouring ones overlapping the transforms.  Asynchronous:
+    synchronise the stream before reading outs."""
+    if outs is None:
+        outs = [empty_pinned(x.shape[0]) for x in xs]
+    assert len(outs) == len(xs)
+    if not xs:
+        return outs
+    lg = _lg(xs[0].shape[0])
+    assert all(x.shape[0] == xs[0].shape[0] and o.shape[0] == x.shape[0] for x, o in zip(xs, outs))
+    ins = (ctypes.c_void_p * len(xs))(*[_hptr(x).value for x in xs])
+    ous = (ctypes.c_void_p * len(xs))(*[_hptr(o).value for o in outs])
+    check(lib().pp_ntt_host_many(ins, ous, len(xs), lg, int(inverse), _stream(stream)))
+    return outs
 
 
 def lde_host(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):

@@ -100,3 +100,47 @@ def test_host_forms_refuse_unpinned_and_device_buffers(pp, cuda):
     st = L.pp_ntt_host(ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(pinned.data_ptr()), 10, 0, None)
     assert st == 1
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("lg,count", [(0, 1), (5, 2), (12, 7), (20, 5)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_ntt_host_many(pp, O, cuda, lg, count, inverse):
+    """pp_ntt_host_many: every polynomial equals its own device transform,
+    with the three device buffers reused (count > 3) and some polynomials in
+    place (h_out[j] == h_in[j])."""
+    import torch
+    P = pp.ppfr
+    xs = [O.random_fr(1 << lg, 0x4A00 + 16 * lg + j) for j in range(count)]
+    hins = [pinned_from(torch, x) for x in xs]
+    outs = [h if j % 3 == 1 else P.empty_pinned(1 << lg) for j, h in enumerate(hins)]
+    s = torch.cuda.Stream()
+    P.ntt_host_many(hins, inverse=inverse, outs=outs, stream=s)
+    s.synchronize()
+    for j, x in enumerate(xs):
+        want = host(P.ntt(dev(x), inverse=inverse))
+        assert np.array_equal(as_u64(outs[j]), want), j
+        if j % 3 != 1:
+            assert np.array_equal(as_u64(hins[j]), x)  # input untouched
+    if lg <= 12:
+        assert O.first_diff(as_u64(outs[-1]), O.ntt(xs[-1], inverse=inverse)) == -1
+
+
+def test_ntt_host_many_refusals(pp, O, cuda):
+    import torch
+    P = pp.ppfr
+    n = 1 << 10
+    x = O.random_fr(n, 0x4B00)
+    good = [pinned_from(torch, x) for _ in range(3)]
+    outs = [torch.zeros((n, 4), dtype=torch.int64, pin_memory=True) for _ in range(3)]
+    assert P.ntt_host_many([], outs=[]) == []  # count 0
+    bad_out = outs[:2] + [torch.zeros((n, 4), dtype=torch.int64)]  # pageable
+    with pytest.raises(P.PPError) as e:
+        P.ntt_host_many(good, outs=bad_out)
+    assert e.value.status == 1
+    torch.cuda.synchronize()
+    # refused before any copy was queued: the good outputs are untouched
+    assert not outs[0].any() and not outs[1].any()
+    P.ntt_host_many(good, outs=outs)
+    torch.cuda.synchronize()
+    want = host(P.ntt(dev(x)))
+    assert all(np.array_equal(as_u64(o), want) for o in outs)
