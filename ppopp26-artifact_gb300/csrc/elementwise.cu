@@ -8,11 +8,12 @@
 // HBM bounds them; grid-stride loops of 16-byte accesses.  Division and
 // inversion differ: the reference inverts each element (mont_t::reciprocal,
 // ff/mont_t.cuh:1117); here a warp's 1024 elements share one inversion
-// (Montgomery's simultaneous inversion: about 3 multiplies per element).  A
-// binary-GCD inversion is ~40K dependent instructions, so fewer of them is
-// what counts: 2^24 divisions took 3.71 ms with one divergent inversion per
-// lane and 32 elements, 5.09 ms with one per warp and 256 elements in
-// registers (118 registers), 1.81 ms as here.  As in the reference, the
+// (Montgomery's simultaneous inversion: about 3 multiplies per element).  An
+// inversion costs thousands of dependent instructions, so fewer of them is
+// what counts: with binary-GCD inversions 2^24 divisions took 3.71 ms with
+// one divergent inversion per lane and 32 elements, 5.09 ms with one per
+// warp and 256 elements in registers (118 registers), 1.81 ms as here; with
+// the divstep inversion (modinv.cuh) 1.73 ms.  As in the reference, the
 // inverse of 0 is taken as 0.
 #include "common.cuh"
 
@@ -73,7 +74,9 @@ __device__ __forceinline__ fr shfl_fr(const fr &v, int src) {
 // trips (the shuffles need all 32).
 constexpr uint32_t kDivRun = 32;
 
-__global__ void __launch_bounds__(kThreads)
+// at most 64 registers: four blocks per SM (with the divstep inversion inlined
+// the compiler would otherwise take 100 and fit two)
+__global__ void __launch_bounds__(kThreads, 4)
     k_fr_div(const fr *a, const fr *b, fr *c, uint64_t n) {
   const int lane = threadIdx.x & 31;
   const uint64_t per_warp = 32ull * kDivRun;
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(kThreads)
     if (lane == 31) suf = fr_one();
     const fr excl = shfl_up_fr(incl, 1);
     // 1 / (this run's product) = (1 / total) * (runs before) * (runs after)
-    fr inv = fr_mul(fr_inv_binary(total), suf);
+    fr inv = fr_mul(fr_inv_fast(total), suf);
     if (lane > 0) inv = fr_mul(inv, excl);
 #pragma unroll 1
     for (int j = (int)kDivRun - 1; j >= 0; --j) {
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // out[0] = 1 / x[0] (0 for 0)
-__global__ void k_fr_inv1(const fr *x, fr *out) { st_fr(out, fr_inv_binary(ld_fr(x))); }
+__global__ void k_fr_inv1(const fr *x, fr *out) { st_fr(out, fr_inv_fast(ld_fr(x))); }
 
 __global__ void __launch_bounds__(kThreads) k_fr_neg(const fr *a, fr *c, uint64_t n) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;

@@ -146,7 +146,7 @@ PP_HD g1a g1x_to_affine(const g1x &p) {
     r.y = fq_zero();
     return r;
   }
-  const fq t = fq_inv(fq_mul(p.zz, p.zzz));  // 1 / (ZZ ZZZ)
+  const fq t = fq_inv_fast(fq_mul(p.zz, p.zzz));  // 1 / (ZZ ZZZ)
   r.x = fq_mul(p.x, fq_mul(t, p.zzz));        // X / ZZ
   r.y = fq_mul(p.y, fq_mul(t, p.zz));         // Y / ZZZ
   return r;

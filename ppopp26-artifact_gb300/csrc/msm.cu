@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(kPointThreads)
       if (!g1x_is_inf(p)) acc = fq_mul(acc, fq_mul(p.zz, p.zzz));
       out[j].x = acc;
     }
-    fq inv = fq_inv(acc);  // acc is a product of non-zero values
+    fq inv = fq_inv_fast(acc);  // acc is a product of non-zero values
     for (uint64_t j = hi; j > lo; --j) {
       const g1x p = q[j - 1];
       g1a a;

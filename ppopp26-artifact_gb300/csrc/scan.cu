@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kScanThreads) k_perm_carry(fr *block_num, fr *
   }
   warp_block_prefix_product(N, s1);
   warp_block_suffix_product(D, s2);  // s2[0]: every denominator (none is zero)
-  if (threadIdx.x == 0) s_inv = fr_inv_binary(s2[0]);
+  if (threadIdx.x == 0) s_inv = fr_inv_fast(s2[0]);
   __syncthreads();
   fr run_n = threadIdx.x ? s1[threadIdx.x - 1] : fr_one();
   fr run_d = fr_mul(s_inv, threadIdx.x + 1 < blockDim.x ? s2[threadIdx.x + 1] : fr_one());

@@ -71,6 +71,28 @@ int main(int argc, char **argv) {
   std::memcpy(b + 20, rm1, 32);
   std::memcpy(a + 28, rm1, 32);
   std::memcpy(b + 28, rm1, 32);
+  // inversion edges (raw word values): 1, 2, 3, 2^k for k = 1 .. 254 in steps
+  // of 23, r - 2, r - 2^32, 2^64 - 1
+  if (n >= 40) {
+    for (int k = 0; k < 3; ++k) {
+      std::memset(a + 4 * (10 + k), 0, 32);
+      a[4 * (10 + k)] = (uint64_t)k + 1;
+    }
+    for (int j = 0, k = 1; k < 255; ++j, k += 23) {
+      uint64_t *p = a + 4 * (13 + j);
+      std::memset(p, 0, 32);
+      p[k / 64] = 1ull << (k % 64);
+    }
+    uint64_t *p = a + 4 * 25;
+    std::memcpy(p, rm1, 32);
+    p[0] -= 1;  // r - 2
+    p = a + 4 * 26;
+    std::memcpy(p, rm1, 32);
+    p[0] = 1;  // r - 2^32
+    p = a + 4 * 27;
+    std::memset(p, 0, 32);
+    p[0] = ~0ull;
+  }
   long bad = 0;
   for (uint64_t i = 0; i < n; ++i) {
     fr x = load(a + 4 * i), y = load(b + 4 * i);
@@ -114,6 +136,16 @@ int main(int argc, char **argv) {
       if (std::memcmp(vb.v, want, 32)) {
         if (bad++ < 5) std::printf("binary inv mismatch at %llu\n", (unsigned long long)i);
       }
+    }
+    if (i < 20000) {
+      or_fr_inv(a + 4 * i, want);
+      // both limb widths: 62 bits (the host form) and 30 bits (the GPU form)
+      fr vf = pp::fr_inv_divsteps<int64_t>(x), vg = pp::fr_inv_divsteps<int32_t>(x);
+      if (std::memcmp(vf.v, want, 32) || std::memcmp(vg.v, want, 32)) {
+        if (bad++ < 5) std::printf("divstep inv mismatch at %llu\n", (unsigned long long)i);
+      }
+    }
+    if (i < 200) {
       uint64_t e[4] = {i * 7919 + 3, 0, 0, 0};
       or_fr_pow(a + 4 * i, e, want);
       fr p = pp::fr_pow_u64(x, e[0]);

@@ -115,6 +115,23 @@ int main(int argc, char **argv) {
       for (const fq &v : e) {
         const fq s1 = fq_sqr(v), s2 = fq_mul(v, v);
         bad += std::memcmp(s1.v, s2.v, 48) != 0;
+        // both inverses agree (0 -> 0), and v * v^-1 = 1 otherwise
+        const fq i1 = fq_inv(v), i2 = fq_inv_divsteps<int64_t>(v);
+        const fq i3 = fq_inv_divsteps<int32_t>(v);
+        bad += std::memcmp(i1.v, i2.v, 48) != 0;
+        bad += std::memcmp(i1.v, i3.v, 48) != 0;
+        if (!fq_is_zero(v)) bad += !fq_eq(fq_mul(v, i2), fq_one());
+      }
+    }
+    // the divstep inverse against the binary GCD on the points' coordinates
+    for (size_t i = 0; i < n; ++i) {
+      const g1a pa = load_aff(&pts[24 * i]);
+      for (const fq *v : {&pa.x, &pa.y}) {
+        const fq i1 = fq_inv(*v), i2 = fq_inv_divsteps<int64_t>(*v);
+        const fq i3 = fq_inv_divsteps<int32_t>(*v);
+        bad += std::memcmp(i1.v, i2.v, 48) != 0;
+        bad += std::memcmp(i1.v, i3.v, 48) != 0;
+        bad += !fq_eq(fq_mul(*v, i2), fq_one());
       }
     }
     std::printf("mismatches %ld\n", bad);
