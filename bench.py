@@ -415,6 +415,8 @@ def secondary_ops(pp, torch):
     constraint_bench(pp, torch, rate, res)
     msm_bench(pp, torch, rate, res)
     res["batched"] = batched_bench(pp, torch)
+    # the launch-bound regime: many small polynomials
+    res["batched_small"] = batched_bench(pp, torch, 1024, 8, 14)
     res["serving"] = serving_bench(pp, torch)
     return res
 
@@ -602,16 +604,20 @@ def msm_bench(pp, torch, rate, res):
     bases.close()
 
 
-def batched_bench(pp, torch):
-    """96 polynomials, sizes log-uniform in 2^12..2^22 (seeded): 64 NTT/INTT,
-    24 lambda=2 LDEs, 8 grand products.  Loop of single calls vs one batch
-    plan (a few persistent launches) vs its CUDA-graph replay."""
+def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22):
+    """count polynomials, sizes log-uniform in 2^lg_lo..2^lg_hi (seeded), in
+    the proportions 2/3 NTT and INTT, 1/4 lambda=2 LDEs, 1/12 grand products
+    (96 polynomials of 2^12..2^22: 64 / 24 / 8).  Loop of single calls vs one
+    batch plan (a few persistent launches) vs its CUDA-graph replay."""
     import numpy as np
 
     P = pp.ppfr
     rng = np.random.default_rng(0xBA7C4)
-    lgs = [int(v) for v in np.floor(rng.uniform(12, 23, 96))]
-    kinds = [P.JOB_NTT] * 32 + [P.JOB_INTT] * 32 + [P.JOB_LDE_COEFFS] * 24 + [P.JOB_GP] * 8
+    lgs = [int(v) for v in np.floor(rng.uniform(lg_lo, lg_hi + 1, count))]
+    n_gp, n_lde = count // 12, count // 4
+    n_ntt = count - n_gp - n_lde
+    kinds = ([P.JOB_NTT] * (n_ntt - n_ntt // 2) + [P.JOB_INTT] * (n_ntt // 2) +
+             [P.JOB_LDE_COEFFS] * n_lde + [P.JOB_GP] * n_gp)
     rng.shuffle(kinds)
     jobs, loop = [], []
     for i, (k, lg) in enumerate(zip(kinds, lgs)):
@@ -631,13 +637,31 @@ def batched_bench(pp, torch):
     l0 = P.launch_count()
     ms_loop = time_device(lambda: [f() for f in loop], 3, 1, torch) / 3
     loop_launches = (P.launch_count() - l0) // 4
+    # the same loop captured in a CUDA graph: no host cost per call, so the
+    # batch plan's gain over it is the device-side one (fewer, fuller launches)
+    ms_loop_graph = None
+    try:
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            [f() for f in loop]  # per-stream workspaces exist before capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            [f() for f in loop]
+        ms_loop_graph = time_device(g.replay, 5, 2, torch) / 5
+        del g
+    except RuntimeError:
+        torch.cuda.synchronize()
     b = P.Batch(jobs)
     info = b.info()
     ms_batch = time_device(b.run, 5, 2, torch) / 5
     b.capture()
     ms_graph = time_device(b.run, 10, 2, torch) / 10
     b.close()
-    return {"polys": 96, "input_elems": elems, "loop_ms": round(ms_loop, 3), "batch_ms": round(ms_batch, 3),
+    return {"polys": count, "lg_range": [lg_lo, lg_hi], "input_elems": elems,
+            "loop_ms": round(ms_loop, 3),
+            "loop_graph_ms": round(ms_loop_graph, 3) if ms_loop_graph else None,
+            "batch_ms": round(ms_batch, 3),
             "graph_ms": round(ms_graph, 3), "loop_launches": int(loop_launches),
             "batch_launches": info["launches"], "speedup_batch": round(ms_loop / ms_batch, 3),
             "speedup_graph": round(ms_loop / ms_graph, 3),

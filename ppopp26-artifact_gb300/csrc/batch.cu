@@ -5,8 +5,9 @@
 //  * every transform is split into its passes (the same radix plans and
 //    tables as single calls); pass p of a job runs at "level" start + p, an
 //    LDE from evaluations chains its INTT and its forward transform;
-//  * one launch per level covers the tiles of every job pass at that level
-//    (k_ntt_batch_level, blocks striding over a prefix-summed tile list);
+//  * one launch per level (per 128 job passes at that level) covers their
+//    tiles (k_ntt_batch_level, blocks striding over a prefix-summed tile
+//    list, the jobs' arguments passed as kernel parameters);
 //  * the grand products run as two launches over the blocks of all of them.
 // A plan owns its descriptors and workspaces (allocated once at creation), so
 // running it allocates nothing and the whole sequence can be captured into a
@@ -24,11 +25,10 @@ namespace pp {
 
 struct BatchPlan {
   int dev = 0;
+  // one level = one launch per chunk of at most kLevelJobs job passes, the
+  // jobs' arguments passed as kernel parameters
   struct Level {
-    PassArgs *d_args = nullptr;
-    uint64_t *d_tile_start = nullptr;
-    uint32_t count = 0;
-    uint64_t total = 0;
+    std::vector<LevelParams> chunks;
   };
   std::vector<Level> levels;
   GpBatchJob *d_gp = nullptr;
@@ -55,10 +55,11 @@ struct SubTransform {
 };
 
 int run_plan(BatchPlan *p, cudaStream_t s) {
-  for (auto &lv : p->levels) {
-    int st = ntt_launch_level(lv.d_args, lv.d_tile_start, lv.count, lv.total, s);
-    if (st) return st;
-  }
+  for (auto &lv : p->levels)
+    for (auto &c : lv.chunks) {
+      int st = ntt_launch_level(c, s);
+      if (st) return st;
+    }
   return gp_batch_launch(p->d_gp, p->d_gp_start, p->gp_count, p->gp_blocks, s);
 }
 
@@ -209,9 +210,6 @@ extern "C" int pp_batch_create(const pp_job *jobs, uint32_t count, void **plan_o
     gstart.push_back(gstart.back() + gg[i].blocks);
   }
   size_t desc_bytes = 0;
-  for (uint32_t L = 0; L < nlevels; ++L)
-    desc_bytes += pp::align_up(lv_args[L].size() * sizeof(pp::PassArgs), 256) +
-                  pp::align_up(lv_start[L].size() * sizeof(uint64_t), 256);
   desc_bytes += pp::align_up(gj.size() * sizeof(pp::GpBatchJob), 256) +
                 pp::align_up(gstart.size() * sizeof(uint32_t), 256);
   char *d_desc = nullptr;
@@ -232,13 +230,22 @@ extern "C" int pp_batch_create(const pp_job *jobs, uint32_t count, void **plan_o
   };
   for (uint32_t L = 0; L < nlevels; ++L) {
     pp::BatchPlan::Level lv;
-    lv.count = (uint32_t)lv_args[L].size();
-    lv.total = lv_start[L].back();
-    lv.d_args = static_cast<pp::PassArgs *>(put(lv_args[L].data(), lv_args[L].size() * sizeof(pp::PassArgs)));
-    lv.d_tile_start = static_cast<uint64_t *>(put(lv_start[L].data(), lv_start[L].size() * sizeof(uint64_t)));
-    p->levels.push_back(lv);
-    p->tiles += lv.total;
-    ++p->launches;
+    const size_t count = lv_args[L].size();
+    for (size_t j0 = 0; j0 < count; j0 += pp::kLevelJobs) {
+      const size_t j1 = std::min(count, j0 + (size_t)pp::kLevelJobs);
+      pp::LevelParams c;
+      std::memset(&c, 0, sizeof(c));
+      c.count = (uint32_t)(j1 - j0);
+      for (size_t j = j0; j < j1; ++j) {
+        c.args[j - j0] = lv_args[L][j];
+        c.tile_start[j - j0] = lv_start[L][j] - lv_start[L][j0];
+      }
+      c.total_tiles = lv_start[L][j1] - lv_start[L][j0];
+      lv.chunks.push_back(c);
+      ++p->launches;
+    }
+    p->tiles += lv_start[L].back();
+    p->levels.push_back(std::move(lv));
   }
   p->gp_count = (uint32_t)gj.size();
   p->gp_blocks = gstart.back();

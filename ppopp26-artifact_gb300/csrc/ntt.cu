@@ -378,21 +378,150 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
 
 // Persistent kernel of one batch level: the tiles of every job pass at this
 // level are numbered consecutively (tile_start = prefix sums over the jobs);
-// blocks stride over them.
-__global__ void __launch_bounds__(256, 2)
-    k_ntt_batch_level(const PassArgs *__restrict__ args, const uint64_t *__restrict__ tile_start,
-                      uint32_t count, uint64_t total_tiles) {
+// blocks stride over them, and a block's job index only moves forward.
+__global__ void __launch_bounds__(256, 2) k_ntt_batch_level(const __grid_constant__ LevelParams p) {
   extern __shared__ uint4 sm[];
-  for (uint64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-    uint32_t lo = 0, hi = count;
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (tile_start[mid] <= t) lo = mid;
-      else hi = mid;
-    }
-    const PassArgs a = args[lo];
-    ntt_tile(a, t - tile_start[lo], sm);
+  uint32_t lo = 0;
+  for (uint64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
+    while (lo + 1 < p.count && p.tile_start[lo + 1] <= t) ++lo;
+    ntt_tile(p.args[lo], t - p.tile_start[lo], sm);
     __syncthreads();  // the next tile reuses the shared memory
+  }
+}
+
+// Transforms of 2^3 .. 2^11 points (single-pass plans) in one block: the
+// input goes to shared memory in bit-reversed order, then radix-2
+// decimation-in-time layers with w_N^(j N / 2m) from the plan's inner table
+// leave the natural-order result.  Transforms this small are bound by
+// latency, not by the multiply pipe.  The tiled pass kernel runs its unrolled
+// radix-8 rounds once over a large code body and waits on instruction fetch
+// (ncu at 2^11: no_instruction stalls 4.3 warps per issue; 46 us per call);
+// this kernel's rolled loops keep its code small.  The input is read in full
+// before anything is written, so in == out is allowed.
+__global__ void __launch_bounds__(512) k_ntt_small(const PassArgs a) {
+  extern __shared__ uint4 sm[];
+  fr *x = reinterpret_cast<fr *>(sm);
+  const uint32_t lg = a.lgN, N = 1u << lg, half = N >> 1;
+#pragma unroll 1
+  for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+    fr v;
+    if (a.in_kind == NTT_IN_SPREAD) {
+      v = (i & ((1u << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (i >> a.spread)) : fr_zero();
+    } else if (i < a.n_valid) {
+      v = ldcs_fr(a.in + i);
+      if (a.in_kind == NTT_IN_DIAG) v = fr_mul(v, ldcs_fr(a.diag + i));
+    } else {
+      v = fr_zero();
+    }
+    st_fr(x + (__brev(i) >> (32 - lg)), v);
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (uint32_t s = 0; s < lg; ++s) {
+#pragma unroll 1
+    for (uint32_t b = threadIdx.x; b < half; b += blockDim.x) {
+      const uint32_t j = b & ((1u << s) - 1);
+      const uint32_t p = ((b >> s) << (s + 1)) + j, q = p + (1u << s);
+      const fr t = fr_mul(ld_fr(x + q), ldg_fr(a.tw_inner + (j << (lg - 1 - s))));
+      const fr u = ld_fr(x + p);
+      st_fr(x + p, fr_add(u, t));
+      st_fr(x + q, fr_sub(u, t));
+    }
+    __syncthreads();
+  }
+#pragma unroll 1
+  for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) {
+    fr v = ld_fr(x + i);
+    if (a.has_post_scale) v = fr_mul(v, a.post_scale);
+    st_fr(a.out + i, v);
+  }
+}
+
+// One tile of a latency-form pass (2^9 .. 2^17 points, one column per tile):
+// the tile geometry, inputs and outputs of ntt_tile, with each column's DFT
+// as rolled radix-2 decimation-in-time layers over its bit-reversed copy in
+// shared memory (so the result is in natural order), canonical throughout.
+__global__ void __launch_bounds__(256) k_ntt_small_pass(const PassArgs a) {
+  extern __shared__ uint4 sm[];
+  fr *x = reinterpret_cast<fr *>(sm);  // column col at x[col R ..]
+  const uint32_t lgR = a.lgR, R = 1u << lgR, T = 1u << a.lgT, E = R << a.lgT;
+  const uint64_t tileid = blockIdx.x;
+  uint64_t base = 0, col0 = 0, in_base = 0, out_base = 0;
+  uint32_t lgS1 = 0;
+  if (!a.last) {
+    const uint32_t lgtpq = a.lgS - a.lgT;
+    const uint64_t q = tileid >> lgtpq, ct = tileid & ((1ull << lgtpq) - 1);
+    col0 = ct << a.lgT;
+    base = (q << (a.lgR + a.lgS)) + col0;
+  } else {
+    const uint32_t lgR1 = a.lgRp[0];
+    lgS1 = a.lgN - lgR1;
+    const uint32_t lgkb = lgR1 - a.lgT;
+    const uint64_t kb = tileid & ((1ull << lgkb) - 1), rest = tileid >> lgkb;
+    uint64_t rin = 0, r = rest;
+    uint32_t acc = lgR1;
+    for (uint32_t j = 1; j + 1 < a.P; ++j) {
+      const uint32_t bits = a.lgRp[j];
+      acc += bits;
+      rin += (r & ((1ull << bits) - 1)) << (a.lgN - acc);
+      r >>= bits;
+    }
+    in_base = ((kb << a.lgT) << lgS1) + rin;
+    out_base = (kb << a.lgT) + (rest << lgR1);
+  }
+#pragma unroll 1
+  for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) {
+    uint32_t n, col;
+    uint64_t g;
+    if (!a.last) {
+      n = e >> a.lgT;
+      col = e & (T - 1);
+      g = base + ((uint64_t)n << a.lgS) + col;
+    } else {
+      n = e & (R - 1);
+      col = e >> a.lgR;
+      g = in_base + ((uint64_t)col << lgS1) + n;
+    }
+    fr v;
+    if (!a.first) {
+      v = ldcs_fr(a.in + g);
+    } else if (a.in_kind == NTT_IN_SPREAD) {
+      v = (g & ((1ull << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (g >> a.spread)) : fr_zero();
+    } else if (g < a.n_valid) {
+      v = ldcs_fr(a.in + g);
+      if (a.in_kind == NTT_IN_DIAG) v = fr_mul(v, ldcs_fr(a.diag + g));
+    } else {
+      v = fr_zero();
+    }
+    st_fr(x + (col << lgR) + (__brev(n) >> (32 - lgR)), v);
+  }
+  __syncthreads();
+  const uint32_t half = E >> 1, hmask = (R >> 1) - 1;
+#pragma unroll 1
+  for (uint32_t s = 0; s < lgR; ++s) {
+#pragma unroll 1
+    for (uint32_t b = threadIdx.x; b < half; b += blockDim.x) {
+      fr *xc = x + ((b >> (lgR - 1)) << lgR);
+      const uint32_t bb = b & hmask, j = bb & ((1u << s) - 1);
+      const uint32_t p = ((bb >> s) << (s + 1)) + j, q = p + (1u << s);
+      const fr t = fr_mul(ld_fr(xc + q), ldg_fr(a.tw_inner + (j << (lgR - 1 - s))));
+      const fr u = ld_fr(xc + p);
+      st_fr(xc + p, fr_add(u, t));
+      st_fr(xc + q, fr_sub(u, t));
+    }
+    __syncthreads();
+  }
+#pragma unroll 1
+  for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) {
+    const uint32_t o = e >> a.lgT, col = e & (T - 1);
+    fr v = ld_fr(x + (col << lgR) + o);
+    if (!a.last) {
+      if (a.tw_layer) v = fr_mul(v, ldcs_fr(a.tw_layer + ((uint64_t)o << a.lgS) + col0 + col));
+      st_fr(a.out + base + ((uint64_t)o << a.lgS) + col, v);
+    } else {
+      if (a.has_post_scale) v = fr_mul(v, a.post_scale);
+      st_fr(a.out + out_base + col + ((uint64_t)o << (a.lgN - a.lgR)), v);
+    }
   }
 }
 
@@ -466,8 +595,9 @@ struct PlanKey {
   int dev;
   uint32_t lgN;
   bool inv;
+  bool small;  // the latency form for single calls of 2^9 .. 2^17 points
   bool operator<(const PlanKey &o) const {
-    return std::tie(dev, lgN, inv) < std::tie(o.dev, o.lgN, o.inv);
+    return std::tie(dev, lgN, inv, small) < std::tie(o.dev, o.lgN, o.inv, o.small);
   }
 };
 
@@ -556,8 +686,11 @@ int get_inner(int dev, uint32_t lgR, bool inv, const fr **out) {
   return PP_OK;
 }
 
-int get_plan(int dev, uint32_t lgN, bool inv, Plan **out) {
-  PlanKey key{dev, lgN, inv};
+// small: two passes of about lgN / 2 bits with one column per tile, so that
+// each pass of a 2^9 .. 2^17-point transform spreads over 16 .. 512 blocks
+// (the throughput plan's 2048-element tiles give 1 .. 64)
+int get_plan(int dev, uint32_t lgN, bool inv, Plan **out, bool small = false) {
+  PlanKey key{dev, lgN, inv, small};
   auto it = g_plans.find(key);
   if (it != g_plans.end()) {
     *out = it->second;
@@ -565,6 +698,7 @@ int get_plan(int dev, uint32_t lgN, bool inv, Plan **out) {
   }
   auto ov = g_split_override.find(lgN);
   std::vector<uint32_t> bits = ov != g_split_override.end() ? ov->second : default_split(lgN);
+  if (small) bits = {lgN - lgN / 2, lgN / 2};
   Plan *p = new Plan();
   p->lgN = lgN;
   p->inverse = inv;
@@ -575,7 +709,7 @@ int get_plan(int dev, uint32_t lgN, bool inv, Plan **out) {
     p->lgR[j] = bits[j];
     acc += bits[j];
     const uint32_t lgS = lgN - acc;
-    if (p->P == 1) {
+    if (p->P == 1 || small) {
       p->lgT[j] = 0;
     } else if (j + 1 < p->P) {
       const uint32_t want = 11 - bits[j];
@@ -621,7 +755,9 @@ int ntt_prepare(uint32_t lg_m, bool inverse) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (lg_m <= 2) return PP_OK;
   Plan *p = nullptr;
-  return get_plan(dev, lg_m, inverse, &p);
+  int st = get_plan(dev, lg_m, inverse, &p);
+  if (!st && ntt_small_form(lg_m)) st = get_plan(dev, lg_m, inverse, &p, true);
+  return st;
 }
 
 int ntt_set_split(uint32_t lg_m, const uint32_t *bits) {
@@ -696,7 +832,7 @@ void ntt_release_tables() {
 
 int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inverse,
                  const NttInputDesc &in, std::vector<PassArgs> &passes,
-                 std::vector<uint64_t> &tiles) {
+                 std::vector<uint64_t> &tiles, bool small) {
   if (lg_m > PP_MAX_LG_N || lg_m < 3) {
     set_error("batched transform of 2^%u points: supported sizes are 2^3 .. 2^%d", lg_m, PP_MAX_LG_N);
     return PP_E_UNSUPPORTED;
@@ -707,13 +843,15 @@ int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool invers
   Plan *plan = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    int st = get_plan(dev, lg_m, inverse, &plan);
+    int st = get_plan(dev, lg_m, inverse, &plan, small);
     if (st) return st;
     if (dev < 64 && !g_attr_set[dev]) {
       PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        2048 * (int)sizeof(fr)));
       PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_batch_level,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2048 * (int)sizeof(fr)));
+      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        2048 * (int)sizeof(fr)));
       g_attr_set[dev] = true;
     }
@@ -761,13 +899,11 @@ int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool invers
   return PP_OK;
 }
 
-int ntt_launch_level(const PassArgs *d_args, const uint64_t *d_tile_start, uint32_t count,
-                     uint64_t total_tiles, cudaStream_t stream) {
-  if (!total_tiles) return PP_OK;
+int ntt_launch_level(const LevelParams &params, cudaStream_t stream) {
+  if (!params.total_tiles) return PP_OK;
   const uint64_t cap = (uint64_t)device_sm_count() * 2;
-  const unsigned grid = (unsigned)(total_tiles < cap ? total_tiles : cap);
-  k_ntt_batch_level<<<grid, 256, 2048 * sizeof(fr), stream>>>(d_args, d_tile_start, count,
-                                                              total_tiles);
+  const unsigned grid = (unsigned)(params.total_tiles < cap ? params.total_tiles : cap);
+  k_ntt_batch_level<<<grid, 256, 2048 * sizeof(fr), stream>>>(params);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
@@ -790,8 +926,9 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
     PP_LAUNCH_CHECK();
     return PP_OK;
   }
-  uint32_t bits[4], np = 0;
-  ntt_get_split(lg_m, bits, &np);
+  const bool small = ntt_small_form(lg_m);
+  uint32_t bits[4], np = 2;
+  if (!small) ntt_get_split(lg_m, bits, &np);
   fr *work = nullptr;
   if (np > 1) {
     int st = PP_OK;
@@ -800,8 +937,25 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
   }
   std::vector<PassArgs> passes;
   std::vector<uint64_t> tiles;
-  int st = ntt_describe(d_in, d_out, work, lg_m, inverse, in, passes, tiles);
+  int st = ntt_describe(d_in, d_out, work, lg_m, inverse, in, passes, tiles, small);
   if (st) return st;
+  if (small) {
+    for (size_t j = 0; j < passes.size(); ++j) {
+      const uint32_t E = 1u << (passes[j].lgR + passes[j].lgT);
+      const uint32_t threads = E / 2 < 32 ? 32 : (E / 2 > 256 ? 256 : E / 2);
+      k_ntt_small_pass<<<(unsigned)tiles[j], threads, E * sizeof(fr), stream>>>(passes[j]);
+      PP_COUNT_LAUNCH();
+      PP_LAUNCH_CHECK();
+    }
+    return PP_OK;
+  }
+  if (passes.size() == 1 && lg_m <= 11) {
+    const uint32_t threads = (uint32_t)(N / 2 < 32 ? 32 : (N / 2 > 512 ? 512 : N / 2));
+    k_ntt_small<<<1, threads, N * sizeof(fr), stream>>>(passes[0]);
+    PP_COUNT_LAUNCH();
+    PP_LAUNCH_CHECK();
+    return PP_OK;
+  }
   for (size_t j = 0; j < passes.size(); ++j) {
     const uint32_t E = 1u << (passes[j].lgR + passes[j].lgT);
     k_ntt_pass<<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(passes[j]);

@@ -57,12 +57,30 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
 
 // Per-pass descriptors (and tile counts) of one transform whose passes use
 // `work` (2^lg_m elements) between them; for batch plans.  lg_m >= 3.
+// small = the latency form of single calls (ntt_small_form); batch plans use
+// the throughput form.
 int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inverse,
                  const NttInputDesc &in, std::vector<PassArgs> &passes,
-                 std::vector<uint64_t> &tiles);
-// One persistent launch over the tiles of `count` job passes (device arrays).
-int ntt_launch_level(const PassArgs *d_args, const uint64_t *d_tile_start, uint32_t count,
-                     uint64_t total_tiles, cudaStream_t stream);
+                 std::vector<uint64_t> &tiles, bool small = false);
+
+// Single calls of 2^9 .. 2^17 points run the latency form: two passes with
+// one column per tile (k_ntt_small_pass).  Those sizes are bound by latency
+// (a few microseconds of work), and the throughput plan's 2048-element tiles
+// would leave most SMs idle.
+inline bool ntt_small_form(uint32_t lg_m) { return lg_m >= 9 && lg_m <= 17; }
+// One persistent launch over the tiles of up to kLevelJobs job passes.  The
+// arguments travel as the kernel's parameters (20.5 KB; CUDA allows 32 KB):
+// the tile code then reads them as constant operands, as k_ntt_pass does,
+// instead of holding them in registers loaded from memory (which made the
+// level kernel 15 % slower per tile than separate pass launches).
+constexpr uint32_t kLevelJobs = 128;
+struct LevelParams {
+  uint64_t tile_start[kLevelJobs];  // job j's tiles are tile_start[j] .. tile_start[j+1]-1
+  PassArgs args[kLevelJobs];
+  uint64_t total_tiles;
+  uint32_t count;
+};
+int ntt_launch_level(const LevelParams &params, cudaStream_t stream);
 
 // Builds (or fetches) the cached tables for a transform size (for graph capture
 // the tables must exist before capture starts).

@@ -64,3 +64,26 @@ def test_batch_graph_replay(pp, cuda):
         for (kind, x, out, lam), ref in zip(jobs, refs):
             assert torch.equal(out, ref), (kind, x.shape[0], lam)
     b.close()
+
+
+def test_batch_more_jobs_than_one_launch_carries(pp, cuda):
+    """300 small jobs: each level needs three launches of at most 128 job
+    passes; every result equals its single call."""
+    torch = cuda
+    P = pp.ppfr
+    rng = np.random.default_rng(77)
+    jobs, refs = [], []
+    for i in range(300):
+        lg = int(rng.integers(3, 12))
+        inverse = bool(i & 1)
+        x = P.random_fr(1 << lg, 5000 + i)
+        jobs.append((P.JOB_INTT if inverse else P.JOB_NTT, x, P.empty(1 << lg), 0))
+        refs.append(P.ntt(x, inverse))
+    b = P.Batch(jobs)
+    assert b.info()["launches"] >= 3
+    for _ in range(2):
+        b.run()
+        torch.cuda.synchronize()
+        for (_, _, out, _), ref in zip(jobs, refs):
+            assert torch.equal(out, ref)
+    b.close()
