@@ -53,7 +53,7 @@ def parse():
                     help="device timing only (no e2e, CPU baseline, ops): the profiling case")
     ap.add_argument("--lg", type=int, default=LG_N, help="transform size (profiling of smaller cases)")
     ap.add_argument("--op", default="ntt",
-                    choices=["ntt", "msm", "msmfixed", "gate", "perm", "gpperm", "scans"],
+                    choices=["ntt", "msm", "msmfixed", "gate", "perm", "gpperm", "scans", "div"],
                     help="with --lean: time one operator alone at 2^lg points (profiling case)")
     return ap.parse_args()
 
@@ -383,19 +383,34 @@ def secondary_ops(pp, torch):
         ms = time_device(fn, reps, 2, torch)
         res[name] = {"ms": round(ms / reps, 4), "Melem_per_s": round(elems * reps / (ms / 1e3) / 1e6, 2)}
 
+    sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s at the maximum SM clock
+
+    def int_frac(name, mm):
+        # algorithmic Montgomery multiplies x 256 multiply instructions
+        res[name]["MM"] = mm
+        res[name]["int_frac_of_nominal_peak"] = round(mm * INSTR_PER_MM / (res[name]["ms"] / 1e3) / peak, 4)
+
     for lg in (22, 26):
         x = pp.random_fr(1 << lg, lg)
         o = ppfr.empty(1 << lg)
         rate("ntt_2^%d" % lg, lambda: pp.ntt(x, out=o), 1 << lg, 3)
+        int_frac("ntt_2^%d" % lg, (1 << lg) // 2 * lg)
         del x, o
     x = pp.random_fr(N, 1)
     o = ppfr.empty(N)
     rate("intt_2^24", lambda: pp.ntt(x, True, out=o), N)
+    int_frac("intt_2^24", N // 2 * LG_N)
     del o
     for lam in (2, 3):
         o = ppfr.empty(N << lam)
+        # coefficients: 2^lam coset transforms of N points plus the N-point
+        # diagonal; evaluations add the N-point INTT
+        coset_mm = (N << lam) // 2 * LG_N + N
         rate("lde_coeffs_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_COEFFS, out=o), N, 3)
+        int_frac("lde_coeffs_2^24_l%d" % lam, coset_mm)
         rate("lde_evals_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_EVALS, out=o), N, 3)
+        int_frac("lde_evals_2^24_l%d" % lam, coset_mm + N // 2 * LG_N)
         del o
     del x
     n = 1 << 20
@@ -503,10 +518,11 @@ def gate_small_constants(ppfr):
 
 
 def profile_op(args, pp, torch):
-    """--lean --op msm|gate|perm|gpperm|scans: one operator at 2^lg points,
-    device time only (the profiling case for ncu launch lists of those
-    kernels).  gpperm is the copy-constraint grand product; scans is one
-    grand product, one evaluation and one division by (X + c)."""
+    """--lean --op msm|gate|perm|gpperm|scans|div: one operator at 2^lg
+    points, device time only (the profiling case for ncu launch lists of
+    those kernels).  gpperm is the copy-constraint grand product; scans is one
+    grand product, one evaluation and one division by (X + c); div is the
+    element-wise division a / b (div_mod)."""
     import numpy as np
 
     ppfr = pp.ppfr
@@ -544,6 +560,10 @@ def profile_op(args, pp, torch):
             ppfr.evaluate(x, pt, out=y)
             work.copy_(x)
             ppfr.div_xplusc_(work, pt)
+    elif args.op == "div":
+        a, b = ppfr.random_fr(n, 0xE1), ppfr.random_fr(n, 0xE2)
+        out = ppfr.empty(n)
+        fn = lambda: ppfr.fr_binary(ppfr.FR_DIV, a, b, out=out)  # noqa: E731
     else:
         vec = [ppfr.random_fr(n, 0xC0 + i) for i in range(13)]
         sca = [ppfr.random_fr(1, 0xD0 + i) for i in range(7)]
