@@ -470,9 +470,9 @@ __device__ g1x dbl_warp(const g1x &p) {
   if (g1x_is_inf(p) || fq_is_zero(p.y)) return g1x_inf();
   const int lane = threadIdx.x & 31;
   const fq u = fq_dbl(p.y);
-  // v = u^2 (lane 0), x2 = x^2 (lane 1)
+  // v = u^2 (lane 0), x2 = x^2 (lane 1): squares on every lane
   fq a = lane == 0 ? u : p.x;
-  fq r = fq_mul(a, a);
+  fq r = fq_sqr(a);
   const fq v = shfl_fq(r, 0), x2 = shfl_fq(r, 1);
   const fq m = fq_add(fq_dbl(x2), x2);
   // w = u v (0), s = x v (1), m^2 (2), zz' = v zz (3)
@@ -508,7 +508,7 @@ __device__ g1x add_warp(const g1x &p, const g1x &q) {
   if (fq_is_zero(P)) return fq_is_zero(R) ? dbl_warp(p) : g1x_inf();
   // P^2 (0), R^2 (1)
   a = lane == 0 ? P : R;
-  r = fq_mul(a, a);
+  r = fq_sqr(a);
   const fq pp = shfl_fq(r, 0), rr = shfl_fq(r, 1);
   // P pp (0), u1 pp (1), zz12 pp (2)
   a = lane == 0 ? P : lane == 1 ? u1 : zz12;
