@@ -386,31 +386,44 @@ def secondary_ops(pp, torch):
     sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     peak = sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s at the maximum SM clock
 
-    def int_frac(name, mm):
-        # algorithmic Montgomery multiplies x 256 multiply instructions
+    hbm = load_peaks()[0].get("hbm_gbs", 6800.0) * 1e9
+
+    def int_frac(name, mm, nbytes=None):
+        # algorithmic Montgomery multiplies x 256 multiply instructions; with
+        # the algorithmic bytes, the roofline time is the larger of the two
+        # bounds and frac_of_roofline = that time / the measured time
+        sec = res[name]["ms"] / 1e3
         res[name]["MM"] = mm
-        res[name]["int_frac_of_nominal_peak"] = round(mm * INSTR_PER_MM / (res[name]["ms"] / 1e3) / peak, 4)
+        res[name]["int_frac_of_nominal_peak"] = round(mm * INSTR_PER_MM / sec / peak, 4)
+        if nbytes is not None:
+            t_int, t_hbm = mm * INSTR_PER_MM / peak, nbytes / hbm
+            res[name].update({"bytes": nbytes, "hbm_frac": round(nbytes / sec / hbm, 4),
+                              "roofline_bound": "int" if t_int >= t_hbm else "hbm",
+                              "frac_of_roofline": round(max(t_int, t_hbm) / sec, 4)})
 
     for lg in (22, 26):
         x = pp.random_fr(1 << lg, lg)
         o = ppfr.empty(1 << lg)
         rate("ntt_2^%d" % lg, lambda: pp.ntt(x, out=o), 1 << lg, 3)
-        int_frac("ntt_2^%d" % lg, (1 << lg) // 2 * lg)
+        int_frac("ntt_2^%d" % lg, (1 << lg) // 2 * lg, 64 << lg)
         del x, o
     x = pp.random_fr(N, 1)
     o = ppfr.empty(N)
     rate("intt_2^24", lambda: pp.ntt(x, True, out=o), N)
-    int_frac("intt_2^24", N // 2 * LG_N)
+    int_frac("intt_2^24", N // 2 * LG_N + N, 64 * N)
     del o
     for lam in (2, 3):
         o = ppfr.empty(N << lam)
         # coefficients: 2^lam coset transforms of N points plus the N-point
         # diagonal; evaluations add the N-point INTT
         coset_mm = (N << lam) // 2 * LG_N + N
-        rate("lde_coeffs_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_COEFFS, out=o), N, 3)
-        int_frac("lde_coeffs_2^24_l%d" % lam, coset_mm)
-        rate("lde_evals_2^24_l%d" % lam, lambda: pp.lde(x, lam, pp.LDE_EVALS, out=o), N, 3)
-        int_frac("lde_evals_2^24_l%d" % lam, coset_mm + N // 2 * LG_N)
+        lde_bytes = 32 * N * (1 + (1 << lam))
+        for form, mode, mm in (("coeffs", pp.LDE_COEFFS, coset_mm),
+                               ("evals", pp.LDE_EVALS, coset_mm + N // 2 * LG_N + N)):
+            name = "lde_%s_2^24_l%d" % (form, lam)
+            rate(name, lambda: pp.lde(x, lam, mode, out=o), N, 3)
+            int_frac(name, mm, lde_bytes)
+            res[name]["out_Melem_per_s"] = round(res[name]["Melem_per_s"] * (1 << lam), 2)
         del o
     del x
     n = 1 << 20
@@ -418,13 +431,17 @@ def secondary_ops(pp, torch):
     z = pp.random_fr(1, 3)
     y = ppfr.empty(1)
     rate("gp_prefix_2^20", lambda: pp.gp_prefix_(p), n, 10)
+    int_frac("gp_prefix_2^20", n, 64 * n)
     rate("eval_2^20", lambda: pp.evaluate(p, z, out=y), n, 10)
+    int_frac("eval_2^20", n, 32 * n)
     rate("div_2^20", lambda: pp.div_xplusc_(p, z), n, 10)
+    int_frac("div_2^20", n, 64 * n)
     w = [pp.random_fr(n, 10 + j) for j in range(3)]
     s = [pp.random_fr(n, 20 + j) for j in range(3)]
     params = pp.random_fr(5, 30)
     zz = ppfr.empty(n)
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
+    int_frac("gp_perm_2^20", 16 * n, 224 * n)
     del w, s, p
     elementwise_bench(pp, torch, rate, res)
     constraint_bench(pp, torch, rate, res)
