@@ -16,8 +16,10 @@ def test_generator_matches_oracle(pp, O, cuda):
         assert (host(pp.random_fr(n, seed, first)) == O.random_fr(n, seed, first)).all()
 
 
-@pytest.mark.parametrize("lg", list(range(0, 17)) + [18, 20])
+@pytest.mark.parametrize("lg", list(range(0, 19)) + [20])
 def test_ntt_bit_exact_all_sizes(pp, O, cuda, lg):
+    """Every size through 2^18: one-block kernel to 2^8, two one-column-tile
+    passes 2^9 .. 2^17, the tiled throughput plan from 2^18."""
     x = pp.random_fr(1 << lg, 100 + lg)
     xh = host(x)
     X = pp.ntt(x)
@@ -82,7 +84,8 @@ def test_ntt_full_size_properties(pp, O, cuda, lg):
     del X, Xh
 
 
-@pytest.mark.parametrize("lg,lam", [(4, 1), (10, 2), (10, 3), (12, 3), (16, 2), (20, 2), (20, 3)])
+@pytest.mark.parametrize("lg,lam", [(4, 1), (6, 2), (7, 2), (10, 2), (10, 3), (12, 3), (15, 2), (16, 2),
+                                    (20, 2), (20, 3)])
 def test_lde_modes_bit_exact(pp, O, cuda, lg, lam):
     x = pp.random_fr(1 << lg, 300 + lg + lam)
     xh = host(x)
