@@ -203,7 +203,7 @@ int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *stream);
 /* -------------------------------------------------------------- batch ---
  * Many polynomials of uneven power-of-two sizes in one plan: every transform
  * job is split into its passes, and each pass level of the whole batch is one
- * persistent launch over the tiles of all jobs at that level; grand products
+ * launch (per 128 jobs) over the tiles of all jobs at that level; grand products
  * run as two launches over all of them.  A plan owns its workspaces and
  * descriptors (allocated by pp_batch_create), so pp_batch_run allocates
  * nothing; pp_batch_capture records the run as a CUDA graph that later

@@ -1,12 +1,12 @@
 // batch.cu -- many polynomials of uneven power-of-two sizes per launch.
 //
 // A batch plan turns a list of jobs (NTT, INTT, the three LDE forms, grand
-// products) into a short, fixed sequence of persistent launches:
+// products) into a short, fixed sequence of launches:
 //  * every transform is split into its passes (the same radix plans and
 //    tables as single calls); pass p of a job runs at "level" start + p, an
 //    LDE from evaluations chains its INTT and its forward transform;
 //  * one launch per level (per 128 job passes at that level) covers their
-//    tiles (k_ntt_batch_level, blocks striding over a prefix-summed tile
+//    tiles (k_ntt_batch_level, one block per tile of a prefix-summed tile
 //    list, the jobs' arguments passed as kernel parameters);
 //  * the grand products run as two launches over the blocks of all of them.
 // A plan owns its descriptors and workspaces (allocated once at creation), so

@@ -376,17 +376,19 @@ __global__ void __launch_bounds__(256, 2) k_ntt_pass(const PassArgs a) {
   ntt_tile(a, blockIdx.x, sm);
 }
 
-// Persistent kernel of one batch level: the tiles of every job pass at this
-// level are numbered consecutively (tile_start = prefix sums over the jobs);
-// blocks stride over them, and a block's job index only moves forward.
+// One batch level: the tiles of every job pass at this level are numbered
+// consecutively (tile_start = prefix sums over the jobs), one block per tile
+// as in k_ntt_pass; a block finds its job by a binary search over the starts.
 __global__ void __launch_bounds__(256, 2) k_ntt_batch_level(const __grid_constant__ LevelParams p) {
   extern __shared__ uint4 sm[];
-  uint32_t lo = 0;
-  for (uint64_t t = blockIdx.x; t < p.total_tiles; t += gridDim.x) {
-    while (lo + 1 < p.count && p.tile_start[lo + 1] <= t) ++lo;
-    ntt_tile(p.args[lo], t - p.tile_start[lo], sm);
-    __syncthreads();  // the next tile reuses the shared memory
+  const uint64_t t = blockIdx.x;
+  uint32_t lo = 0, hi = p.count;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (p.tile_start[mid] <= t) lo = mid;
+    else hi = mid;
   }
+  ntt_tile(p.args[lo], t - p.tile_start[lo], sm);
 }
 
 // Transforms of 2^3 .. 2^11 points (single-pass plans) in one block: the
@@ -901,9 +903,11 @@ int ntt_describe(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool invers
 
 int ntt_launch_level(const LevelParams &params, cudaStream_t stream) {
   if (!params.total_tiles) return PP_OK;
-  const uint64_t cap = (uint64_t)device_sm_count() * 2;
-  const unsigned grid = (unsigned)(params.total_tiles < cap ? params.total_tiles : cap);
-  k_ntt_batch_level<<<grid, 256, 2048 * sizeof(fr), stream>>>(params);
+  if (params.total_tiles > 0x7fffffffull) {
+    set_error("batch level of %llu tiles exceeds one launch", (unsigned long long)params.total_tiles);
+    return PP_E_UNSUPPORTED;
+  }
+  k_ntt_batch_level<<<(unsigned)params.total_tiles, 256, 2048 * sizeof(fr), stream>>>(params);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
