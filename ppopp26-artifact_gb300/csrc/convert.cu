@@ -55,9 +55,12 @@ __global__ void __launch_bounds__(kThreads) k_count_noncanonical(const fr *in, u
 
 bool aligned16(const void *p) { return p && (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// one thread per element (the loops stride only past 2^31 - 1 blocks), as
+// for the element-wise operators, where capping the grid at 8 blocks per SM
+// cost 3-6 %
 unsigned grid_for(uint64_t n) {
   const uint64_t want = (n + kThreads - 1) / kThreads;
-  const uint64_t cap = (uint64_t)device_sm_count() * 8;
+  const uint64_t cap = 0x7fffffffull;
   return (unsigned)(want < cap ? want : cap);
 }
 

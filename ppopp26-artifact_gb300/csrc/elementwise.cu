@@ -23,9 +23,12 @@ namespace {
 constexpr int kThreads = 256;
 constexpr uint32_t kPowRun = 128;  // powers: elements per thread after one x^lo
 
+// one thread per unit of work, the loops striding only past 2^31 - 1 blocks:
+// at 2^24 add / mul / x^5 take 0.228 / 0.336 / 1.255 ms, against 0.243 /
+// 0.348 / 1.289 ms with the grid capped at 8 blocks per SM
 unsigned grid_for(uint64_t work) {
   const uint64_t want = (work + kThreads - 1) / kThreads;
-  const uint64_t cap = (uint64_t)device_sm_count() * 8;
+  const uint64_t cap = 0x7fffffffull;
   return (unsigned)(want < cap ? (want ? want : 1) : cap);
 }
 
