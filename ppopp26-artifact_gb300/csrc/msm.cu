@@ -599,9 +599,12 @@ MsmLayout msm_layout(uint64_t n, const MsmPlan &p) {
   return L;
 }
 
-unsigned grid_for(uint64_t work, int threads, int per_sm) {
+// one thread per unit of work (loops stride only past 2^31 - 1 blocks): 2^20
+// points took 13.77 ms, against 14.09 ms with grids capped at 8-16 blocks
+// per SM
+unsigned grid_for(uint64_t work, int threads) {
   const uint64_t want = (work + threads - 1) / threads;
-  const uint64_t cap = (uint64_t)device_sm_count() * per_sm;
+  const uint64_t cap = 0x7fffffffull;
   return (unsigned)(want < cap ? (want ? want : 1) : cap);
 }
 
@@ -685,11 +688,11 @@ int msm_run(const g1a *points, const uint32_t *scalars, uint64_t n, const MsmPla
 
   // 1-3: signed digits, bucket sizes, counting sort of (point, sign) by bucket
   PP_CUDA_TRY(cudaMemsetAsync(counts, 0, nb * 4, s));
-  k_msm_digits<<<grid_for(n, 256, 8), 256, 0, s>>>(scalars, n, p, digits, counts);
+  k_msm_digits<<<grid_for(n, 256), 256, 0, s>>>(scalars, n, p, digits, counts);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   if ((st = scan_u32(counts, nb, offsets, cursor, tiles, s))) return st;
-  k_msm_scatter<<<grid_for((uint64_t)p.W * n, 256, 8), 256, 0, s>>>(digits, n, p, cursor, list);
+  k_msm_scatter<<<grid_for((uint64_t)p.W * n, 256), 256, 0, s>>>(digits, n, p, cursor, list);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
 
@@ -700,12 +703,12 @@ int msm_run(const g1a *points, const uint32_t *scalars, uint64_t n, const MsmPla
   for (uint32_t lv = 0; lv < L.levels; ++lv) {
     uint32_t *next = u32(L.next[lv & 1]), *noff = u32(L.noff[lv & 1]);
     g1x *part_out = pts(L.part[lv & 1]);
-    k_msm_groups<<<grid_for(nb, 256, 8), 256, 0, s>>>(m, nb, groups, next);
+    k_msm_groups<<<grid_for(nb, 256), 256, 0, s>>>(m, nb, groups, next);
     PP_COUNT_LAUNCH();
     PP_LAUNCH_CHECK();
     if ((st = scan_u32(groups, nb, goff, nullptr, tiles, s))) return st;
     if ((st = scan_u32(next, nb, noff, nullptr, tiles, s))) return st;
-    k_msm_level<<<grid_for((uint64_t)p.W * n / 4 + nb, kPointThreads, 16), kPointThreads, 0, s>>>(
+    k_msm_level<<<grid_for((uint64_t)p.W * n / 4 + nb, kPointThreads), kPointThreads, 0, s>>>(
         points, lv == 0 ? list : nullptr, part_in, m, off, goff, noff,
         (uint32_t)nb, part_out, buckets);
     PP_COUNT_LAUNCH();
@@ -716,11 +719,11 @@ int msm_run(const g1a *points, const uint32_t *scalars, uint64_t n, const MsmPla
   }
 
   // 5-7: weighted bucket sums per bucket set, sets combined, affine result
-  k_msm_segments<<<grid_for((uint64_t)p.nsets * p.S, kPointThreads, 16), kPointThreads, 0, s>>>(
+  k_msm_segments<<<grid_for((uint64_t)p.nsets * p.S, kPointThreads), kPointThreads, 0, s>>>(
       buckets, p, seg_t, seg_r);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  k_msm_bitsums<<<grid_for((uint64_t)p.nsets * chunk_counts(p).ncw, kPointThreads, 16), kPointThreads,
+  k_msm_bitsums<<<grid_for((uint64_t)p.nsets * chunk_counts(p).ncw, kPointThreads), kPointThreads,
                   0, s>>>(seg_t, seg_r, p, chunks);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
@@ -833,10 +836,10 @@ extern "C" int pp_msm_g1_bases_create(const void *d_points, uint64_t n, uint32_t
               cudaGetErrorString(cudaGetLastError()));
   }
   for (uint64_t w = 1; st == PP_OK && w < W; ++w) {
-    k_msm_table_double<<<grid_for(n, kPointThreads, 16), kPointThreads, 0, s>>>(table + (w - 1) * n,
+    k_msm_table_double<<<grid_for(n, kPointThreads), kPointThreads, 0, s>>>(table + (w - 1) * n,
                                                                                n, c, tmp);
     PP_COUNT_LAUNCH();
-    k_msm_table_affine<<<grid_for((n + kTableRun - 1) / kTableRun, kPointThreads, 16), kPointThreads,
+    k_msm_table_affine<<<grid_for((n + kTableRun - 1) / kTableRun, kPointThreads), kPointThreads,
                          0, s>>>(tmp, n, table + w * n);
     PP_COUNT_LAUNCH();
     const cudaError_t e = cudaGetLastError();
@@ -934,7 +937,7 @@ extern "C" int pp_g1_mul_gen(const void *d_scalars, uint64_t n, void *d_out, voi
     set_error("pp_g1_mul_gen: buffers must be 16-byte aligned device pointers");
     return PP_E_INVAL;
   }
-  k_g1_mul_gen<<<grid_for(n, kPointThreads, 16), kPointThreads, 0, (cudaStream_t)stream>>>(
+  k_g1_mul_gen<<<grid_for(n, kPointThreads), kPointThreads, 0, (cudaStream_t)stream>>>(
       static_cast<const uint32_t *>(d_scalars), n, static_cast<g1a *>(d_out));
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
