@@ -118,41 +118,51 @@ __device__ __forceinline__ fr delta4_6(const fr &x) {
 // written first, then the arithmetic and public-input terms and the fixed-
 // and variable-base group additions are added.
 
-// Stages the scalars (and three one two) in shared memory and returns whether
-// four, one, two, three, nine, eighteen, eightyone and eightythree hold those
-// integers, as the prover passes them.  Then the kernels take SMALL = true:
-// multiplies by them become additions and one one / three one two drop out,
-// with the same field values (2^22 points: range and logic 47 -> 27
+// The scalars as the gate kernels use them, prepared once per call by
+// k_gate_prepare: the PP_GATE_NS scalars, then three one two, then whether
+// four, one, two, three, nine, eighteen, eightyone and eightythree hold
+// those integers, as the prover passes them.  Then the kernels take
+// SMALL = true: multiplies by them become additions and one one / three one
+// two drop out, with the same field values (range and logic 47 -> 27
 // multiplies per point, groups 38 -> 35).  Any other values take SMALL =
-// false, the expression as written.  Every thread gets the same answer.
-__device__ __forceinline__ bool stage_scalars(const GateArgs &a, fr *sc) {
-  __shared__ int s_small;
-  if (threadIdx.x < PP_GATE_NS) sc[threadIdx.x] = ldg_fr(a.s[threadIdx.x]);
+// false, the expression as written.
+struct GateScalars {
+  fr s[PP_GATE_NS + 1];
+  int small;
+};
+
+__global__ void k_gate_prepare(const GateArgs a, GateScalars *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  fr sc[PP_GATE_NS + 1];
+  for (int j = 0; j < PP_GATE_NS; ++j) sc[j] = ldg_fr(a.s[j]);
+  sc[PP_GATE_NS] = fr_mul(fr_mul(sc[PP_GATE_S_THREE], sc[PP_GATE_S_ONE]), sc[PP_GATE_S_TWO]);
+  const fr one = fr_one();
+  out->small = fr_eq(sc[PP_GATE_S_ONE], one) && fr_eq(sc[PP_GATE_S_TWO], dbl(one)) &&
+               fr_eq(sc[PP_GATE_S_THREE], mul3(one)) && fr_eq(sc[PP_GATE_S_FOUR], mul4(one)) &&
+               fr_eq(sc[PP_GATE_S_NINE], mul9(one)) && fr_eq(sc[PP_GATE_S_EIGHTEEN], mul18(one)) &&
+               fr_eq(sc[PP_GATE_S_EIGHTYONE], mul81(one)) &&
+               fr_eq(sc[PP_GATE_S_EIGHTYTHREE], mul83(one));
+  for (int j = 0; j <= PP_GATE_NS; ++j) st_fr(out->s + j, sc[j]);
+}
+
+// copies the prepared scalars to shared memory
+__device__ __forceinline__ void stage_scalars(const GateScalars *g, fr *sc) {
+  if (threadIdx.x <= PP_GATE_NS) sc[threadIdx.x] = ldg_fr(g->s + threadIdx.x);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    sc[PP_GATE_NS] =
-        fr_mul(fr_mul(sc[PP_GATE_S_THREE], sc[PP_GATE_S_ONE]), sc[PP_GATE_S_TWO]);
-    const fr one = fr_one();
-    s_small = fr_eq(sc[PP_GATE_S_ONE], one) && fr_eq(sc[PP_GATE_S_TWO], dbl(one)) &&
-              fr_eq(sc[PP_GATE_S_THREE], mul3(one)) && fr_eq(sc[PP_GATE_S_FOUR], mul4(one)) &&
-              fr_eq(sc[PP_GATE_S_NINE], mul9(one)) && fr_eq(sc[PP_GATE_S_EIGHTEEN], mul18(one)) &&
-              fr_eq(sc[PP_GATE_S_EIGHTYONE], mul81(one)) &&
-              fr_eq(sc[PP_GATE_S_EIGHTYTHREE], mul83(one));
-  }
-  __syncthreads();
-  return s_small != 0;
 }
 
 #define S(name) sc[PP_GATE_S_##name]
 #define V(name) ldcs_fr(a.v[PP_GATE_V_##name] + i)
 
 // The host launches both forms; the one whose SMALL does not match the
-// scalars returns after staging them.
+// scalars returns at once.
 template <bool SMALL>
-__global__ void __launch_bounds__(kThreads, 2) k_gate_range_logic(const GateArgs a, fr *out,
+__global__ void __launch_bounds__(kThreads, 2) k_gate_range_logic(const GateArgs a,
+                                                               const GateScalars *gs, fr *out,
                                                                uint64_t n) {
+  if ((__ldg(&gs->small) != 0) != SMALL) return;
   __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
-  if (stage_scalars(a, sc) != SMALL) return;
+  stage_scalars(gs, sc);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const fr k312 = sc[PP_GATE_NS];
@@ -222,9 +232,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_gate_arith(const GateArgs a, fr
 }
 
 template <bool SMALL>
-__global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a, fr *out, uint64_t n) {
+__global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a,
+                                                          const GateScalars *gs, fr *out,
+                                                          uint64_t n) {
+  if ((__ldg(&gs->small) != 0) != SMALL) return;
   __shared__ __align__(16) fr sc[PP_GATE_NS + 1];
-  if (stage_scalars(a, sc) != SMALL) return;
+  stage_scalars(gs, sc);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const fr a_ = V(A), b = V(B), c = V(C), d = V(D);
@@ -265,10 +278,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_gate_groups(const GateArgs a, f
 
 bool aligned16(const void *p) { return p && (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-// capped: at most 8 blocks per SM, each striding over points (the gate
-// kernels that stage their scalars once per block); otherwise one thread per
-// point (the permutation terms: 2^22 points in 1.45 ms, against 1.85 ms with
-// the cap; the gate's arithmetic kernel, which stages nothing)
+// capped: at most 8 blocks per SM, each striding over points; otherwise one
+// thread per point, as every kernel here launches (the permutation terms:
+// 2^22 points in 1.45 ms, against 1.85 ms with the cap)
 unsigned grid_for(uint64_t n, bool capped = true) {
   const uint64_t want = (n + kThreads - 1) / kThreads;
   const uint64_t cap = capped ? (uint64_t)device_sm_count() * 8 : 0x7fffffffull;
@@ -378,26 +390,30 @@ extern "C" int pp_gate_constraint(const pp_gate_args *a, void *d_out, uint64_t n
     g.s[j] = static_cast<const pp::fr *>(a->s[j]);
   }
   g.sbox_alpha = (uint32_t)a->sbox_alpha;
-  const unsigned grid = pp::grid_for(n);
-  // each pair: the form that does not match the scalars returns at once
-  pp::k_gate_range_logic<true><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
-      g, static_cast<pp::fr *>(d_out), n);
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = PP_OK;
+  auto *gs = static_cast<pp::GateScalars *>(pp::workspace_get(sizeof(pp::GateScalars), s, 8, &st));
+  if (st) return st;
+  pp::k_gate_prepare<<<1, 32, 0, s>>>(g, gs);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gate_range_logic<false><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
-      g, static_cast<pp::fr *>(d_out), n);
+  // one thread per point; of each pair, the form that does not match the
+  // scalars returns at once
+  const unsigned grid = pp::grid_for(n, false);
+  pp::fr *out = static_cast<pp::fr *>(d_out);
+  pp::k_gate_range_logic<true><<<grid, pp::kThreads, 0, s>>>(g, gs, out, n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gate_arith<<<pp::grid_for(n, false), pp::kThreads, 0, (cudaStream_t)stream>>>(
-      g, static_cast<pp::fr *>(d_out), n);
+  pp::k_gate_range_logic<false><<<grid, pp::kThreads, 0, s>>>(g, gs, out, n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gate_groups<true><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
-      g, static_cast<pp::fr *>(d_out), n);
+  pp::k_gate_arith<<<grid, pp::kThreads, 0, s>>>(g, out, n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
-  pp::k_gate_groups<false><<<grid, pp::kThreads, 0, (cudaStream_t)stream>>>(
-      g, static_cast<pp::fr *>(d_out), n);
+  pp::k_gate_groups<true><<<grid, pp::kThreads, 0, s>>>(g, gs, out, n);
+  PP_COUNT_LAUNCH();
+  PP_LAUNCH_CHECK();
+  pp::k_gate_groups<false><<<grid, pp::kThreads, 0, s>>>(g, gs, out, n);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
