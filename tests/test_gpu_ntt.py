@@ -59,14 +59,16 @@ def test_ntt_of_delta_is_reference_root_table(pp, O, cuda, golden):
         assert (Xi[1] == want).all()
 
 
-@pytest.mark.parametrize("lg", [22, 24])
+@pytest.mark.parametrize("lg", [19, 21, 22, 23, 24])
 def test_ntt_full_size_bit_exact(pp, O, cuda, lg):
+    """Every throughput-plan size through 2^24 with its shipped radix split
+    (2^19: 10+9, 2^21: 6+6+9, 2^23: 9+6+8 ...) against the oracle."""
     x = pp.random_fr(1 << lg, 0x5EED0000 + lg)
     X = pp.ntt(x)
     assert O.first_diff(host(X), O.ntt(host(x))) == -1
 
 
-@pytest.mark.parametrize("lg", [24, 26])
+@pytest.mark.parametrize("lg", [24, 25, 26])
 def test_ntt_full_size_properties(pp, O, cuda, lg):
     """Round trip and X[k] = p(w^k) at sampled k (first, last, random)."""
     import torch
