@@ -24,7 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "libpporacle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libppref.so")
-REF_SRC = os.environ.get("PP_REFERENCE_SRC", "/root/reference")
+# the reference sources: $PP_REFERENCE_SRC, else the copy staged by
+# ``make -C oracle stage REF_CHECKOUT=<checkout>``
+REF_SRC = os.environ.get("PP_REFERENCE_SRC", os.path.join(HERE, "_ref", "src"))
 
 R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
 RMONT = 1 << 256

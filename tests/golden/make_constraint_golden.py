@@ -161,4 +161,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: %s <reference checkout>" % sys.argv[0])
+    main(sys.argv[1])
