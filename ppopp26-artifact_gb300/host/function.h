@@ -27,15 +27,8 @@
 #pragma once
 #include <cstdint>
 
+#include "fr_cpu.h"  // cpu::BLS12_381_Fr_G1, the reference's host field element
 #include "syncedmem.h"
-
-namespace cpu {
-// the reference's CPU field element (PLONK/utils/mont/cpu/ff/bls12-381.hpp:
-// 28-32): 4 little-endian 64-bit limbs, Montgomery form
-struct BLS12_381_Fr_G1 {
-  uint64_t limb[4];
-};
-}  // namespace cpu
 
 SyncedMemory accumulate_mul_poly(SyncedMemory product, cudaStream_t stream = (cudaStream_t)0);
 void accumulate_mul_poly_(SyncedMemory product, SyncedMemory output,
