@@ -1,6 +1,7 @@
 """NTT / INTT / LDE on the GPU through the C ABI, bit-exact against the oracle
-(small and medium sizes) and through size-independent properties at the
-benchmark sizes (2^22, 2^24, 2^26)."""
+at every size through 2^24, at the benchmark sizes (NTT/INTT 2^22, 2^24,
+2^26; LDE 2^22 and 2^24 at lambda = 2, 3 in both coset forms), and through
+size-independent properties at 2^25."""
 from __future__ import annotations
 
 import numpy as np
@@ -68,11 +69,22 @@ def test_ntt_full_size_bit_exact(pp, O, cuda, lg):
     assert O.first_diff(host(X), O.ntt(host(x))) == -1
 
 
-@pytest.mark.parametrize("lg", [24, 25, 26])
-def test_ntt_full_size_properties(pp, O, cuda, lg):
-    """Round trip and X[k] = p(w^k) at sampled k (first, last, random)."""
+@pytest.mark.parametrize("lg", [22, 24, 26])
+def test_ntt_intt_benchmark_sizes_bit_exact(pp, O, cuda, lg):
+    """The benchmark sizes, forward and inverse, every element against the
+    oracle (which takes a few seconds per transform on 16 host cores)."""
+    n = 1 << lg
+    x = pp.random_fr(n, 0xA11CE + lg)
+    xh = host(x)
+    assert O.first_diff(host(pp.ntt(x)), O.ntt(xh)) == -1
+    assert O.first_diff(host(pp.intt(x)), O.ntt(xh, inverse=True)) == -1
+
+
+def test_ntt_2p25_properties(pp, O, cuda):
+    """2^25: round trip and X[k] = p(w^k) at sampled k (first, last, random)."""
     import torch
 
+    lg = 25
     n = 1 << lg
     x = pp.random_fr(n, 0xA11CE + lg)
     X = pp.ntt(x)
@@ -96,17 +108,15 @@ def test_lde_modes_bit_exact(pp, O, cuda, lg, lam):
     assert O.first_diff(host(pp.lde(x, lam, pp.LDE_SPREAD)), O.lde_spread(xh, lam)) == -1
 
 
-@pytest.mark.parametrize("lam", [2, 3])
-def test_lde_full_size_properties(pp, O, cuda, lam):
-    """2^24 coefficients: sampled outputs equal p(h w_L^k), h = 7^(2^lam)."""
-    lg = 24
-    x = pp.random_fr(1 << lg, 0x1DE + lam)
-    out = pp.lde(x, lam, pp.LDE_COEFFS)
+@pytest.mark.parametrize("lg,lam", [(22, 2), (22, 3), (24, 2), (24, 3)])
+def test_lde_benchmark_sizes_bit_exact(pp, O, cuda, lg, lam):
+    """The benchmark LDE sizes in both coset forms, every one of the
+    2^(lg+lam) outputs against the oracle: from coefficients (shift
+    7^(2^lam)) and from evaluations (INTT, then shift 7)."""
+    x = pp.random_fr(1 << lg, 0x1DE0 + 16 * lg + lam)
     xh = host(x)
-    oh = host(out)
-    wL = O.root_of_unity(lg + lam)
-    h = O.fr_pow(O.mont(7), 1 << lam)
-    rng = np.random.default_rng(lam)
-    for k in [0, 1, (1 << (lg + lam)) - 1] + [int(v) for v in rng.integers(0, 1 << (lg + lam), 2)]:
-        wk = O.fr_pow(wL, k)
-        assert (O.evaluate(xh, O.fr_mul(h, wk)) == oh[k]).all(), k
+    out = host(pp.lde(x, lam, pp.LDE_COEFFS))
+    assert O.first_diff(out, O.lde_coeffs(xh, lam)) == -1
+    del out
+    out = host(pp.lde(x, lam, pp.LDE_EVALS))
+    assert O.first_diff(out, O.lde_evals(xh, lam)) == -1
