@@ -432,6 +432,12 @@ int pp_copy_to_host(void *h_dst, const void *d_src, uint64_t bytes);
 /* number of kernel launches this library has issued from the calling process */
 uint64_t pp_launch_count(void);
 
+/* number of device allocations (cudaMalloc, cudaMallocAsync,
+ * cudaMallocFromPoolAsync) this library has requested in the calling process;
+ * a diagnostic with no counterpart in the reference, which lets a caller check
+ * that a call allocated nothing */
+uint64_t pp_device_alloc_count(void);
+
 /* drop cached tables and workspaces of the current device (synchronises it) */
 int pp_release(void);
 

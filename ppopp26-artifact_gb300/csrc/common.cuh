@@ -67,5 +67,9 @@ void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status);
 // counts kernel launches issued by this library (pp_launch_count)
 void count_launch();
 #define PP_COUNT_LAUNCH() ::pp::count_launch()
+// every device allocation this library requests (cudaMalloc, cudaMallocAsync,
+// cudaMallocFromPoolAsync) is counted; pp_device_alloc_count() reads the total
+void count_alloc();
+#define PP_COUNT_ALLOC() ::pp::count_alloc()
 
 }  // namespace pp

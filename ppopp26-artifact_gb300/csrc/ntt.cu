@@ -640,6 +640,7 @@ int build_windows(const fr &base, fr **d_win) {
     for (int t = 0; t < 10; ++t) s = fr_sqr(s);  // step^(2^10)
     step = s;
   }
+  PP_COUNT_ALLOC();
   PP_CUDA_TRY(cudaMalloc(d_win, 3072 * sizeof(fr)));
   PP_CUDA_TRY(cudaMemcpy(*d_win, w.data(), 3072 * sizeof(fr), cudaMemcpyHostToDevice));
   return PP_OK;
@@ -651,6 +652,7 @@ int build_table(fr **out, uint64_t count, const fr &base, uint32_t kind, uint32_
   fr *win = nullptr;
   int st = build_windows(base, &win);
   if (st) return st;
+  PP_COUNT_ALLOC();
   cudaError_t e = cudaMalloc(out, count * sizeof(fr));
   if (e != cudaSuccess) {
     cudaFree(win);

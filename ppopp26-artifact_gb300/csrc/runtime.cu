@@ -14,6 +14,7 @@ namespace pp {
 namespace {
 thread_local char t_err[512] = "";
 std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_allocs{0};
 
 struct WsKey {
   int dev;
@@ -40,6 +41,7 @@ void set_error(const char *fmt, ...) {
 const char *last_error() { return t_err; }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 
 int device_sm_count() {
   static int cached[64] = {0};
@@ -74,6 +76,7 @@ void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status) {
     b.ptr = nullptr;
     b.bytes = 0;
   }
+  PP_COUNT_ALLOC();
   cudaError_t e = cudaMalloc(&b.ptr, bytes);
   if (e != cudaSuccess) {
     b.ptr = nullptr;
@@ -121,6 +124,8 @@ const char *pp_last_error(void) { return pp::last_error(); }
 const char *pp_version(void) { return "ppfr 0.1 (sm_103a)"; }
 
 uint64_t pp_launch_count(void) { return pp::g_launches.load(); }
+
+uint64_t pp_device_alloc_count(void) { return pp::g_allocs.load(); }
 
 int pp_release(void) { return pp::release_all(); }
 

@@ -15,6 +15,8 @@
 //     or after it (division) and each thread replays its chunk with the exact
 //     carry; evaluation composes all block maps in one block.
 // Field arithmetic is exact, so the grouping does not change any result.
+#include <cuda.h>
+
 #include "common.cuh"
 #include "ntt.cuh"
 #include "scan.cuh"
@@ -681,9 +683,48 @@ static_assert((uint64_t)kEvalNoAllocMaxBlocks * kScanThreads * kEvalNoAllocChunk
 // [0, 1024): affine-map offsets a_b of the blocks, [1024, 2048): factors b_b
 static __device__ __align__(256) fr g_eval_noalloc_scratch[2 * kEvalNoAllocMaxBlocks];
 
-// device address of g_eval_noalloc_scratch, looked up once per device
+// Device address of g_eval_noalloc_scratch per device, with the id of the CUDA
+// context it was looked up in.  A device reset (cudaDeviceReset) destroys the
+// primary context and the module with it; the next context loads the module
+// again, possibly elsewhere, under a new context id.  So the cached address is
+// used only while the calling thread's current context has the stored id, and
+// looked up again otherwise.
+struct NoAllocAddr {
+  unsigned long long ctx_id = 0;
+  fr *addr = nullptr;
+};
 static std::mutex g_eval_noalloc_mu;
-static fr *g_eval_noalloc_addr[64] = {nullptr};
+static NoAllocAddr g_eval_noalloc_addr[64];
+
+// Id of the calling thread's current CUDA context (cuCtxGetCurrent + cuCtxGetId,
+// reached through the runtime's driver entry points so that the library does
+// not link the driver library), or 0 when there is none or it cannot be read.
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+      get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 }  // namespace pp
 
@@ -715,10 +756,13 @@ extern "C" int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, 
   }
   fr *scratch = nullptr;
   {
-    // set-up on the first call on this device (that device is current): the
-    // host-side name of the array is not a device address; ask the runtime
+    // set-up on the first call on this device (that device is current), and
+    // again after its context changed: the host-side name of the array is not
+    // a device address; ask the runtime
     std::lock_guard<std::mutex> lk(pp::g_eval_noalloc_mu);
-    if (!pp::g_eval_noalloc_addr[dev]) {
+    pp::NoAllocAddr &slot = pp::g_eval_noalloc_addr[dev];
+    const unsigned long long ctx_id = pp::current_context_id();
+    if (!slot.addr || ctx_id == 0 || slot.ctx_id != ctx_id) {
       void *p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, pp::g_eval_noalloc_scratch);
       if (e != cudaSuccess) {
@@ -726,9 +770,11 @@ extern "C" int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, 
         pp::set_error("pp_eval_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
         return PP_E_CUDA;
       }
-      pp::g_eval_noalloc_addr[dev] = static_cast<fr *>(p);
+      slot.addr = static_cast<fr *>(p);
+      // the look-up makes the device's primary context current if none was
+      slot.ctx_id = ctx_id ? ctx_id : pp::current_context_id();
     }
-    scratch = pp::g_eval_noalloc_addr[dev];
+    scratch = slot.addr;
   }
   pp::ScanGeom g;
   g.n = n;

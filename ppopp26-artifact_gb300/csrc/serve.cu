@@ -91,6 +91,7 @@ int launch_bundle(Server *S, Bundle &b) {
   cudaStream_t s = S->streams[b.slot];
   const uint32_t lg = b.req.lg_n, lam = b.req.lambda;
   const size_t n = size_t{1} << lg;
+  PP_COUNT_ALLOC();
   cudaError_t e = cudaMallocFromPoolAsync(&b.mem, b.bytes, S->pool, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
