@@ -39,7 +39,7 @@ N = 1 << LG_N
 MM_PER_NTT = (N // 2) * LG_N          # algorithmic Montgomery multiplies (radix-2 count)
 INSTR_PER_MM = 256                     # 8x8 limbs: 4 n^2 integer multiply instructions
 BYTES_PER_NTT = 2 * 32 * N             # read + write once
-IMAD_PER_CLK_PER_SM = 64               # 32-bit multiply-add lanes per SM per clock (measured)
+IMAD_PER_CLK_PER_SM = 64               # 32-bit multiply-add lanes per SM per clock (nominal)
 
 
 def parse():
@@ -142,6 +142,23 @@ def profile_traffic(name: str):
     return None
 
 
+def measure_int_rates(ppfr):
+    """Measured integer-pipe rates of this GPU (pp_measure_int_rates), the
+    denominators of the integer roofline: lane operations per second of
+    mad.lo.u32 / mad.hi.u32 / mad.wide.u32 loops at full occupancy, and the
+    standalone Montgomery multiply rate."""
+    import ctypes
+
+    L = ppfr.lib()
+    f = L.pp_measure_int_rates
+    f.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    f.restype = ctypes.c_int
+    out = (ctypes.c_double * 4)()
+    ppfr.check(f(out))
+    return {"mad_lo_per_s": out[0], "mad_hi_per_s": out[1], "mad_wide_per_s": out[2],
+            "mont_mul_per_s": out[3]}
+
+
 def reduce_max_over_ranks(values, dist, device):
     """Element-wise maximum of this rank's timings (ms) over all ranks: the
     slowest rank sets every whole-job rate.  dist is torch.distributed (or
@@ -194,8 +211,10 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    reps = max(1, args.steps // 10)
-    for _ in range(min(args.warmup, 1)):
+    # one step = one full 2^24 NTT of the CPU implementation (about 1.5 s on
+    # 16 Arm cores); warm-up steps at 2^20 load and warm the library
+    reps = max(1, min(args.steps, 200))
+    for _ in range(args.warmup):
         cpu_ntt_rate(20, 1, threads)
     rate, dt = cpu_ntt_rate(LG_N, reps, threads)
     line = {
@@ -203,7 +222,9 @@ def run_reference(args, rank, world):
         "unit": "Melem/s", "n_gpus": args.gpus, "steps": reps, "warmup": args.warmup,
         "ms_per_step": round(dt / reps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32x8 (Fr, Montgomery)", "data": "synthetic (seeded SplitMix64 Fr)",
-        "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N},
+        "config": {"workload": "ntt forward 2^24, natural order in/out", "lg_n": LG_N,
+                   "l2_flush": "not needed: 512 MiB input > 129 MB L2",
+                   "parallelism": "replicas" if args.gpus > 1 else "1 GPU"},
         "cpu_baseline": {"value": round(rate, 3), "unit": "Melem/s", "cores": threads, "kind": "port",
                          "sample": "%d full 2^24 NTTs (oracle restatement; the reference has no CPU NTT)" % reps},
         "e2e": {"value": round(rate, 3), "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -319,9 +340,10 @@ def run_ours(args, rank, world, local):
         e2e_value, e2e_form = e2e_stream_value, (
             "streamed (pp_ntt_host_many): H2D / NTT / D2H of neighbouring steps overlap on 3 streams")
 
+    rates = measure_int_rates(ppfr)
     ops = {}
     if not args.no_ops and rank == 0:
-        ops = secondary_ops(pp, torch)
+        ops = secondary_ops(pp, torch, rates["mad_lo_per_s"])
 
     if rank != 0:
         if dist:
@@ -330,7 +352,8 @@ def run_ours(args, rank, world, local):
     peaks, peak_kind = load_peaks()
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count
-    int_peak = n_sm * IMAD_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12  # T instr / s
+    nominal_int_peak = n_sm * IMAD_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12  # T instr / s
+    int_peak = rates["mad_lo_per_s"] / 1e12  # measured in this run
     sec_per_ntt = ms / args.steps / 1e3
     achieved_int = MM_PER_NTT * INSTR_PER_MM / sec_per_ntt / 1e12
     achieved_hbm = BYTES_PER_NTT / sec_per_ntt / 1e9
@@ -352,13 +375,18 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "int", "kernel": "k_ntt_pass", "achieved": round(achieved_int, 3),
                      "peak": round(int_peak, 3), "unit": "Tinstr/s", "frac": round(achieved_int / int_peak, 4),
+                     "peak_kind": "measured in this run: mad.lo.u32 lane operations/s of a full-occupancy "
+                                  "loop (pp_measure_int_rates)",
+                     "nominal_peak": round(nominal_int_peak, 3),
+                     "frac_of_nominal": round(achieved_int / nominal_int_peak, 4),
+                     "measured_rates_T_per_s": {k: round(v / 1e12, 4) for k, v in rates.items()},
                      "traffic": traffic,
                      "mixed_rate_ceiling": round(int_peak * 2 / 3, 3),
                      "frac_of_mixed_rate_ceiling": round(achieved_int / (int_peak * 2 / 3), 4),
                      "note": "algorithmic (N/2)lgN Montgomery multiplies x 256 32-bit multiply instructions; "
-                             "peak = SMs x 64 multiply lanes/clk x median SM clock under load (the low-half "
-                             "rate); half of the 256 are high halves at half that rate, so 2/3 of peak is "
-                             "the ceiling for any multiply built from them"},
+                             "peak = the measured low-half (mad.lo) rate; half of the 256 are high halves, "
+                             "which run at half that rate, so 2/3 of peak is the ceiling for any multiply "
+                             "built from them"},
         "roofline_hbm": {"bound": "hbm", "achieved": round(achieved_hbm, 2), "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": round(achieved_hbm / peaks.get("hbm_gbs", 6800.0), 4),
                          "peak_kind": peak_kind},
@@ -372,8 +400,9 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
-def secondary_ops(pp, torch):
-    """Quick device timings of the other operators (inputs resident)."""
+def secondary_ops(pp, torch, int_peak=None):
+    """Quick device timings of the other operators (inputs resident).
+    int_peak: the measured mad.lo lane-operation rate (instr / s)."""
     import numpy as np
 
     ppfr = pp.ppfr
@@ -384,7 +413,7 @@ def secondary_ops(pp, torch):
         res[name] = {"ms": round(ms / reps, 4), "Melem_per_s": round(elems * reps / (ms / 1e3) / 1e6, 2)}
 
     sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s at the maximum SM clock
+    peak = int_peak or sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s
 
     hbm = load_peaks()[0].get("hbm_gbs", 6800.0) * 1e9
 
@@ -394,7 +423,7 @@ def secondary_ops(pp, torch):
         # bounds and frac_of_roofline = that time / the measured time
         sec = res[name]["ms"] / 1e3
         res[name]["MM"] = mm
-        res[name]["int_frac_of_nominal_peak"] = round(mm * INSTR_PER_MM / sec / peak, 4)
+        res[name]["int_frac_of_peak"] = round(mm * INSTR_PER_MM / sec / peak, 4)
         if nbytes is not None:
             t_int, t_hbm = mm * INSTR_PER_MM / peak, nbytes / hbm
             res[name].update({"bytes": nbytes, "hbm_frac": round(nbytes / sec / hbm, 4),
@@ -443,14 +472,36 @@ def secondary_ops(pp, torch):
     rate("gp_perm_2^20", lambda: pp.gp_perm(w, s, params, out=zz), n, 10)
     int_frac("gp_perm_2^20", 16 * n, 224 * n)
     del w, s, p
+    host_resident_bench(pp, torch, rate, res)
     elementwise_bench(pp, torch, rate, res)
-    constraint_bench(pp, torch, rate, res)
-    msm_bench(pp, torch, rate, res)
+    constraint_bench(pp, torch, rate, res, peak)
+    msm_bench(pp, torch, rate, res, peak)
     res["batched"] = batched_bench(pp, torch)
     # the launch-bound regime: many small polynomials
     res["batched_small"] = batched_bench(pp, torch, 1024, 8, 14)
     res["serving"] = serving_bench(pp, torch)
     return res
+
+
+def host_resident_bench(pp, torch, rate, res):
+    """The reference's own host-resident configurations, page-locked host
+    input and output: our_ntt at 2^22, 2^24, 2^26 (ntt.cu:1193-1206) against
+    pp_ntt_host, and our_lde at 2^20, 2^22, 2^24 with lambda = 2, 3
+    (lde.cu:1550-1580; coefficients in) against pp_lde_host.  Events bracket
+    the whole call, as the reference's own timers do."""
+    ppfr = pp.ppfr
+    hin = ppfr.empty_pinned(1 << 26)
+    hin.copy_(ppfr.random_fr(1 << 26, 0x4057).cpu())
+    hout = ppfr.empty_pinned(1 << 27)
+    for lg in (22, 24, 26):
+        x, o = hin[:1 << lg], hout[:1 << lg]
+        rate("ntt_host_2^%d" % lg, lambda: ppfr.ntt_host(x, out=o), 1 << lg, 3)
+    for lg in (20, 22, 24):
+        for lam in (2, 3):
+            x, o = hin[:1 << lg], hout[:1 << (lg + lam)]
+            name = "lde_host_2^%d_l%d" % (lg, lam)
+            rate(name, lambda: ppfr.lde_host(x, lam, pp.LDE_COEFFS, out=o), 1 << lg, 3)
+    del hin, hout
 
 
 def elementwise_bench(pp, torch, rate, res):
@@ -474,15 +525,13 @@ def elementwise_bench(pp, torch, rate, res):
     del a, b, c
 
 
-def constraint_bench(pp, torch, rate, res):
+def constraint_bench(pp, torch, rate, res, peak):
     """Quotient-constraint operators over 2^22 extended-domain points (the 8x
     LDE of a 2^19-row circuit), with the integer-pipe fraction of each:
     18 Montgomery multiplies per point for the fused permutation terms and 104
     for the gate terms at sbox_alpha = 5, 256 multiply instructions each."""
     ppfr = pp.ppfr
     n = 1 << 22
-    sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6  # instr / s at the maximum SM clock
 
     def vec(i):
         return ppfr.random_fr(n, 0xC0 + i)
@@ -516,7 +565,7 @@ def constraint_bench(pp, torch, rate, res):
               "gate_constraint_2^22_general_scalars"):
         pts = res[k]["Melem_per_s"] * 1e6
         mm = res[k]["MM_per_point"]
-        res[k]["int_frac_of_nominal_peak"] = round(pts * mm * 256 / peak, 4)
+        res[k]["int_frac_of_peak"] = round(pts * mm * 256 / peak, 4)
 
 
 def gate_small_constants(ppfr):
@@ -605,12 +654,12 @@ def msm_points(ppfr, n):
     return base.repeat(reps, 1)[:n].contiguous()
 
 
-def msm_bench(pp, torch, rate, res):
+def msm_bench(pp, torch, rate, res, peak):
     """G1 multi-scalar multiplication of 2^20 points (msm_points); the
     scalars are seeded random canonical Fr values.  Integer fraction: W n
     mixed additions of ~10 Fq Montgomery multiplies (W = 256 / c + 1
     windows), each 4 * 12^2 = 576 32-bit multiply instructions, against the
-    nominal integer peak.  The fixed-base form times pp_msm_g1_fixed on
+    measured integer peak.  The fixed-base form times pp_msm_g1_fixed on
     window tables built once, outside the timed region."""
     ppfr = pp.ppfr
     n = 1 << 20
@@ -621,11 +670,9 @@ def msm_bench(pp, torch, rate, res):
     rate(name, lambda: ppfr.msm_g1(pts, sc, out=out), n, 3)
     c = ppfr.msm_window_bits(n)
     windows = 256 // c + 1
-    sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    peak = sm * IMAD_PER_CLK_PER_SM * 2070e6
     instr = windows * n * 10 * 576
     res[name].update({"window_bits": c, "windows": windows,
-                      "int_frac_of_nominal_peak": round(instr / (res[name]["ms"] / 1e3) / peak, 4),
+                      "int_frac_of_peak": round(instr / (res[name]["ms"] / 1e3) / peak, 4),
                       "points": "1024 distinct generator multiples, tiled"})
     torch.cuda.synchronize()
     t0 = time.perf_counter()

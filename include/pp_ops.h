@@ -69,6 +69,13 @@ int pp_ntt_autotune(uint32_t lg_n, int reps, uint32_t *best_bits4, float *best_m
 int pp_tune_save(const char *path);
 int pp_tune_load(const char *path);
 
+/* Measured integer-pipe rates of the current GPU, the denominators of the
+ * integer roofline: out[0] mad.lo.u32, out[1] mad.hi.u32, out[2] mad.wide.u32
+ * (64-bit addend) lane operations per second, each from a full-occupancy loop
+ * of independent chains; out[3] standalone Montgomery multiplies per second.
+ * No counterpart in the reference.  About 30 ms of GPU time. */
+int pp_measure_int_rates(double out[4]);
+
 /* ---------------------------------------------------------------- LDE ---
  * Low-degree extension onto 2^(lg_n+lambda) points, natural order out.
  *  mode 0 (PP_LDE_COEFFS): d_in holds 2^lg_n coefficients a_i; output is

@@ -28,11 +28,11 @@ namespace pp {
 // Blocks per SM each operator's geometry aims for (scan_geom): longer chunks
 // cut the summaries to scan, more blocks hide more latency.  Swept over 1, 2,
 // 4, 8 and 16 on GB300 at 2^20 / 2^22 elements: grand product 2 (80.0 us
-// against 86.5 for 4; 4 is 3 % faster at 2^22), evaluation 2 (58 / 121
-// against 68 / 128), division 2 (94.5 / 222 against 128 / 252), permutation
-// product 8 (574 / 2125 against 592 / 2180; its local pass runs 2 blocks per
-// SM, so it needs more of them to hide latency).
-constexpr uint32_t kGpBlocksPerSm = 2, kEvalBlocksPerSm = 2, kDivBlocksPerSm = 2,
+// against 86.5 for 4; 4 is 3 % faster at 2^22), division 2 (94.5 / 222
+// against 128 / 252), permutation product 8 (574 / 2125 against 592 / 2180;
+// its local pass runs 2 blocks per SM, so it needs more of them to hide
+// latency).  Evaluation has its own geometry (k_eval_tree).
+constexpr uint32_t kGpBlocksPerSm = 2, kDivBlocksPerSm = 2,
                    kPermBlocksPerSm = 8;
 
 // ---------------------------------------------------------------- helpers
@@ -45,20 +45,51 @@ constexpr uint32_t kGpBlocksPerSm = 2, kEvalBlocksPerSm = 2, kDivBlocksPerSm = 2
 // scans (9 dependent steps instead of 16) made the 2^20 grand product,
 // evaluation and division 13-36 % slower on GB300.
 
-// inclusive prefix product over the block (commutative); afterwards s[t]
-// holds thread t's inclusive product, which is also returned
+// prod p[i], lo <= i < hi (hi > lo), in ascending order
+__device__ __forceinline__ fr chunk_product(const fr *p, uint64_t lo, uint64_t hi) {
+  fr acc = ld_fr(p + lo);
+  for (uint64_t i = lo + 1; i < hi; ++i) acc = fr_mul(acc, ld_fr(p + i));
+  return acc;
+}
+
+// Horner value sum_{lo <= i < hi} p[i] m^(i - lo) (hi > lo), from the top
+__device__ __forceinline__ fr chunk_horner(const fr *p, uint64_t lo, uint64_t hi, const fr &m) {
+  fr acc = ld_fr(p + hi - 1);
+  for (uint64_t i = hi - 1; i > lo; --i) acc = fr_add(ld_fr(p + i - 1), fr_mul(m, acc));
+  return acc;
+}
+
+// inclusive prefix product over a block of 256 threads (commutative);
+// afterwards s[t] holds thread t's inclusive product, which is also returned.
+// A work-efficient up-sweep over the lowest three tree levels leaves the
+// products of the 32 runs of 8; one warp scans those with shuffles (5 steps),
+// and a three-level down-sweep hands the run prefixes back down.  12
+// dependent multiplies against 17 for the full up- and down-sweep: the block
+// scan is latency-bound (few threads multiply at each level).
+__device__ __forceinline__ fr shfl_up_fr(const fr &v, int o);
+
 __device__ fr block_prefix_product(fr v, fr *s) {
-  const int t = threadIdx.x, n = blockDim.x;
+  const int t = threadIdx.x;
+  constexpr int n = kScanThreads;
+  static_assert(kScanThreads == 256, "32 runs of 8");
   s[t] = v;
   __syncthreads();
-  for (int d = 1; d < n; d <<= 1) {
+  for (int d = 1; d < 8; d <<= 1) {
     const int idx = (t + 1) * 2 * d - 1;
     if (idx < n) s[idx] = fr_mul(s[idx - d], s[idx]);
     __syncthreads();
   }
-  if (t == 0) s[n - 1] = fr_one();
+  if (t < 32) {
+    fr inc = s[8 * t + 7];
+    for (int o = 1; o < 32; o <<= 1) {
+      const fr u = shfl_up_fr(inc, o);
+      if (t >= o) inc = fr_mul(u, inc);
+    }
+    const fr ex = shfl_up_fr(inc, 1);
+    s[8 * t + 7] = t ? ex : fr_one();
+  }
   __syncthreads();
-  for (int d = n >> 1; d >= 1; d >>= 1) {
+  for (int d = 4; d >= 1; d >>= 1) {
     const int idx = (t + 1) * 2 * d - 1;
     if (idx < n) {
       const fr left = s[idx - d];
@@ -147,21 +178,35 @@ __device__ fr warp_block_suffix_product(fr v, fr *s) {
 // (sa[t], sb[t]) = F_t for every t; without `all` only F_0 is produced (in
 // thread 0's (a, b) and sa[0], sb[0]).  Scanned in reversed order u = n-1-t,
 // where the running composition is G_u = g_u o G_{u-1}.
+// NAMED: the block also has a helper warp past the first 256 threads that
+// does not take part, so the scan synchronises its 256 threads on a named
+// barrier instead of __syncthreads.
+template <bool NAMED>
+__device__ __forceinline__ void scan_sync() {
+  if (NAMED) asm volatile("bar.sync 1, 256;" ::: "memory");
+  else __syncthreads();
+}
+
+template <bool NAMED = false>
 __device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb, bool all = true) {
-  const int t = threadIdx.x, n = blockDim.x;
+  const int t = threadIdx.x, n = NAMED ? kScanThreads : blockDim.x;
   const int u = n - 1 - t;
   sa[u] = a;
   sb[u] = b;
-  __syncthreads();
+  scan_sync<NAMED>();
+  // The full scan of 256 maps takes the hybrid form of block_prefix_product:
+  // three up-sweep levels, one warp scanning the 32 run maps, three
+  // down-sweep levels.
+  const bool hybrid = all && n == 256;
   // combine(left = earlier in u, right = later in u) = right o left
-  for (int d = 1; d < n; d <<= 1) {
+  for (int d = 1; d < (hybrid ? 8 : n); d <<= 1) {
     const int idx = (t + 1) * 2 * d - 1;
     if (idx < n) {
       const fr la = sa[idx - d], lb = sb[idx - d], ra = sa[idx], rb = sb[idx];
       sa[idx] = fr_add(ra, fr_mul(rb, la));
       sb[idx] = fr_mul(rb, lb);
     }
-    __syncthreads();
+    scan_sync<NAMED>();
   }
   if (!all) {
     // sa[n-1], sb[n-1] = G_{n-1} = F_0
@@ -171,15 +216,30 @@ __device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb, bool all = tru
       sa[0] = a;
       sb[0] = b;
     }
-    __syncthreads();
+    scan_sync<NAMED>();
     return;
   }
-  if (t == 0) {
+  if (hybrid) {
+    if (t < 32) {
+      // exclusive scan of the run maps at u = 8k + 7, in u order
+      fr xa = sa[8 * t + 7], xb = sb[8 * t + 7];
+      for (int o = 1; o < 32; o <<= 1) {
+        const fr ua = shfl_up_fr(xa, o), ub = shfl_up_fr(xb, o);
+        if (t >= o) {
+          xa = fr_add(xa, fr_mul(xb, ua));
+          xb = fr_mul(xb, ub);
+        }
+      }
+      const fr ea = shfl_up_fr(xa, 1), eb = shfl_up_fr(xb, 1);
+      sa[8 * t + 7] = t ? ea : fr_zero();
+      sb[8 * t + 7] = t ? eb : fr_one();
+    }
+  } else if (t == 0) {
     sa[n - 1] = fr_zero();
     sb[n - 1] = fr_one();
   }
-  __syncthreads();
-  for (int d = n >> 1; d >= 1; d >>= 1) {
+  scan_sync<NAMED>();
+  for (int d = hybrid ? 4 : n >> 1; d >= 1; d >>= 1) {
     const int idx = (t + 1) * 2 * d - 1;
     if (idx < n) {
       const fr la = sa[idx - d], lb = sb[idx - d], pa = sa[idx], pb = sb[idx];
@@ -188,17 +248,17 @@ __device__ void block_affine_suffix(fr &a, fr &b, fr *sa, fr *sb, bool all = tru
       sa[idx] = fr_add(la, fr_mul(lb, pa));  // left o P
       sb[idx] = fr_mul(lb, pb);
     }
-    __syncthreads();
+    scan_sync<NAMED>();
   }
   // exclusive E_u in (sa[u], sb[u]); inclusive G_u = g_u o E_u = F_t
   const fr ea = sa[u], eb = sb[u];
   const fr ia = fr_add(a, fr_mul(b, ea)), ib = fr_mul(b, eb);
-  __syncthreads();
+  scan_sync<NAMED>();
   sa[t] = ia;
   sb[t] = ib;
   a = ia;
   b = ib;
-  __syncthreads();
+  scan_sync<NAMED>();
 }
 
 // ------------------------------------------------------------ grand product
@@ -207,8 +267,7 @@ __device__ __forceinline__ void gp_local_body(const fr *__restrict__ in, const S
                                               fr *__restrict__ block_total, uint32_t blk, fr *s) {
   const uint64_t gt = blk * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k, hi = lo + g.k < g.n ? lo + g.k : g.n;
-  fr p = fr_one();
-  for (uint64_t i = lo; i < hi; ++i) p = fr_mul(p, ld_fr(in + i));
+  const fr p = lo < hi ? chunk_product(in, lo, hi) : fr_one();
   const fr incl = block_prefix_product(p, s);
   // exclusive = inclusive of the previous thread
   const fr excl = threadIdx.x ? s[threadIdx.x - 1] : fr_one();
@@ -421,37 +480,36 @@ __global__ void __launch_bounds__(kScanThreads)
 
 // --------------------------------------------- backward affine recurrence
 // S_i = p_i + m * S_{i+1}: a thread's chunk [lo, hi) is the map
-// S_lo = L + m^(hi-lo) * S_hi with L its Horner value.
-// m_k = m^k for the full chunk length k, shared by the block: only a shorter
-// (last) chunk computes its own power.
-__device__ __forceinline__ void chunk_map(const fr *p, uint64_t lo, uint64_t hi, uint64_t k,
-                                          const fr &m, const fr &m_k, fr &a, fr &b) {
-  fr L = fr_zero();
-  for (uint64_t i = hi; i > lo; --i) L = fr_add(ld_fr(p + i - 1), fr_mul(m, L));
-  a = L;
-  b = hi - lo == k ? m_k : hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
-}
+// S_lo = L + m^(hi-lo) * S_hi with L its Horner value.  m^K for the full
+// chunk length K is shared by the block: only a shorter (last) chunk computes
+// its own power.
 
-// per-thread exclusive suffix map (optional) and per-block map
-__global__ void __launch_bounds__(kScanThreads) k_affine_local(const fr *__restrict__ p, ScanGeom g,
-                                                                const fr *__restrict__ m_ptr,
-                                                                int negate_m, fr *thread_a,
-                                                                fr *thread_b, fr *block_a,
-                                                                fr *block_b) {
+// per-thread exclusive suffix map (optional) and per-block map.  Launched
+// with kScanThreads + 32 threads: the extra warp computes m^K while the
+// others run their chunks' Horner chains, which do not need it.
+__global__ void __launch_bounds__(kScanThreads + 32) k_affine_local(const fr *__restrict__ p, ScanGeom g,
+                                                                     const fr *__restrict__ m_ptr,
+                                                                     int negate_m, fr *thread_a,
+                                                                     fr *thread_b, fr *block_a,
+                                                                     fr *block_b) {
   __shared__ fr sa[kScanThreads], sb[kScanThreads];
   __shared__ fr s_mk;
   fr m = ld_fr(m_ptr);
   if (negate_m) m = fr_neg(m);
-  if (threadIdx.x == 0) s_mk = fr_pow_u64(m, g.k);
-  __syncthreads();
+  if (threadIdx.x >= kScanThreads) {
+    if (threadIdx.x == kScanThreads) s_mk = fr_pow_u64(m, g.k);
+    __syncthreads();
+    return;  // the scan below synchronises the other 256 threads by name
+  }
   const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
   const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
-  fr a, b;
-  chunk_map(p, lo, hi, g.k, m, s_mk, a, b);
-  block_affine_suffix(a, b, sa, sb, thread_a != nullptr);
+  const fr L = hi > lo ? chunk_horner(p, lo, hi, m) : fr_zero();
+  __syncthreads();  // m^K ready
+  fr a = L, b = hi - lo == g.k ? s_mk : hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
+  block_affine_suffix<true>(a, b, sa, sb, thread_a != nullptr);
   if (thread_a && gt < g.threads) {
-    const bool last = threadIdx.x == blockDim.x - 1;
+    const bool last = threadIdx.x == kScanThreads - 1;
     st_fr(thread_a + gt, last ? fr_zero() : sa[threadIdx.x + 1]);
     st_fr(thread_b + gt, last ? fr_one() : sb[threadIdx.x + 1]);
   }
@@ -512,6 +570,108 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
   if (threadIdx.x == 0) st_fr(y, A);
 }
 
+// ------------------------------------------------------------ evaluation
+// y = sum_i p_i x^i in one launch.
+//  * Thread t of the grid takes the K contiguous coefficients from t K and
+//    runs Horner over them: L_t = sum_{i<K} p_{tK+i} x^i.  K is chosen as for
+//    the other scans (scan_geom, two blocks per SM).
+//  * A block folds its 256 values pairwise, L_u + x^(K s) L_{u+s} for
+//    s = 1, 2, 4, ..., 128: V_b = sum_t L_t x^(K t), one multiply per fold.
+//  * The block that finishes last (a ticket counter) folds the block values
+//    the same way with the weights x^(T 2^j), T = 256 K, into y.
+// Every weight is (x^K)^(2^i) for some i, so a ninth warp of each block
+// computes x^K and then the squaring chain while the other eight run their
+// Horner chains: the weights of the block fold (i < 8) are ready by the time
+// the chains end, and the rest before the block's last barrier.
+// The fold's grouping of the sum does not change the value: field addition is
+// exact.
+constexpr uint32_t kEvalBlocksPerSm = 2;
+constexpr uint32_t kEvalMaxPow = 48;
+
+__device__ __forceinline__ fr ldcg_fr(const fr *p) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(p);
+  uint4 a = __ldcg(q), b = __ldcg(q + 1);
+  return fr{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w}};
+}
+
+// barrier of the 256 folding threads (warps 0-7); the power warp stays out
+__device__ __forceinline__ void fold_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// sv[0] := sum_u sv[u] w^u folded over 256 values, where the fold at
+// distance 2^j uses pw[first + j] = w^(2^j)
+__device__ __forceinline__ void fold256(fr *sv, const fr *pw, uint32_t first) {
+  const uint32_t tid = threadIdx.x;
+#pragma unroll 1
+  for (uint32_t j = 0; j < 8; ++j) {
+    if (tid < (kScanThreads >> (j + 1))) {
+      const uint32_t u = tid << (j + 1);
+      sv[u] = fr_add(sv[u], fr_mul(pw[first + j], sv[u + (1u << j)]));
+    }
+    fold_sync();
+  }
+}
+
+// g: K = g.k coefficients per thread; lg_per: each thread of the last block
+// folds 2^lg_per block values; the weights pw[i] = x^(K 2^i),
+// i < npow = 8 + lg_per + 8, are needed
+__global__ void __launch_bounds__(kScanThreads + 32)
+    k_eval_tree(const fr *__restrict__ p, ScanGeom g, const fr *__restrict__ xp, uint32_t lg_per,
+                uint32_t npow, fr *__restrict__ block_val, uint32_t *__restrict__ ticket,
+                fr *__restrict__ y) {
+  __shared__ fr pw[kEvalMaxPow];
+  __shared__ fr sv[kScanThreads];
+  __shared__ uint32_t s_last;
+  const uint32_t tid = threadIdx.x;
+  const fr x = ld_fr(xp);
+  fr v = x;  // the power warp's running square
+  if (tid >= kScanThreads) {
+    // the power warp: one lane computes x^K and the weights of the block fold
+    if (tid == kScanThreads) {
+      v = fr_pow_u64(x, g.k);
+      pw[0] = v;
+      for (uint32_t i = 1; i < 8; ++i) {
+        v = fr_mul(v, v);
+        pw[i] = v;
+      }
+    }
+  } else {
+    const uint64_t lo = ((uint64_t)blockIdx.x * kScanThreads + tid) * g.k;
+    fr L = fr_zero();
+    if (lo < g.n) L = chunk_horner(p, lo, lo + g.k < g.n ? lo + g.k : g.n, x);
+    sv[tid] = L;
+  }
+  __syncthreads();  // the block fold's weights and the chunk values are ready
+  if (tid == kScanThreads) {
+    // the rest of the chain, for the last block's fold, during the block fold
+    for (uint32_t i = 8; i < npow; ++i) {
+      v = fr_mul(v, v);
+      pw[i] = v;
+    }
+  }
+  if (tid < kScanThreads) fold256(sv, pw, 0);
+  if (tid == 0) {
+    st_fr(block_val + blockIdx.x, sv[0]);
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || tid >= kScanThreads) return;
+  // last block: fold the gridDim.x block values, y = sum_b V_b x^(T b)
+  __threadfence();
+  const uint32_t nb = gridDim.x;
+  const uint64_t b0 = (uint64_t)tid << lg_per;
+  fr V = fr_zero();
+  for (uint64_t b = b0 + (1ull << lg_per); b > b0; --b)
+    if (b - 1 < nb) V = fr_add(ldcg_fr(block_val + b - 1), fr_mul(pw[8], V));
+  sv[tid] = V;
+  fold_sync();
+  fold256(sv, pw, 8 + lg_per);
+  if (tid == 0) {
+    st_fr(y, sv[0]);
+    *ticket = 0;
+  }
+}
+
 __global__ void k_zero1(fr *y) { st_fr(y, fr_zero()); }
 
 static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
@@ -568,7 +728,7 @@ extern "C" int pp_div_xplusc(void *d_inout, uint64_t n, const void *d_c, void *s
   if (st) return st;
   fr *ta = ws, *tb = ws + g.threads, *ba = ws + 2 * g.threads, *bb = ba + g.blocks;
   const fr *c = static_cast<const fr *>(d_c);
-  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(static_cast<const fr *>(d_inout), g, c,
+  pp::k_affine_local<<<g.blocks, pp::kScanThreads + 32, 0, s>>>(static_cast<const fr *>(d_inout), g, c,
                                                            1, ta, tb, ba, bb);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
@@ -593,15 +753,24 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
     return PP_OK;
   }
   const pp::ScanGeom g = pp::scan_geom(n, pp::kEvalBlocksPerSm);
+  const uint32_t nb = g.blocks;
+  uint32_t lg_per = 0;
+  while (((uint64_t)pp::kScanThreads << lg_per) < nb) ++lg_per;
+  const uint32_t npow = 8 + lg_per + 8;
+  if (npow > pp::kEvalMaxPow) {
+    pp::set_error("pp_eval: %llu coefficients are too many", (unsigned long long)n);
+    return PP_E_UNSUPPORTED;
+  }
   int st = PP_OK;
-  fr *ws = static_cast<fr *>(pp::workspace_get(2 * g.blocks * sizeof(fr), s, 1, &st));
+  // block values, then the ticket counter in its own 32-byte slot
+  char *ws = static_cast<char *>(pp::workspace_get((nb + 1) * sizeof(fr), s, 1, &st));
   if (st) return st;
-  fr *ba = ws, *bb = ws + g.blocks;
-  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(
-      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), 0, nullptr, nullptr, ba, bb);
-  PP_COUNT_LAUNCH();
-  PP_LAUNCH_CHECK();
-  pp::k_eval_final<<<1, pp::kScanThreads, 0, s>>>(ba, bb, g.blocks, static_cast<fr *>(d_y));
+  fr *block_val = reinterpret_cast<fr *>(ws);
+  uint32_t *ticket = reinterpret_cast<uint32_t *>(ws + nb * sizeof(fr));
+  PP_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
+  pp::k_eval_tree<<<nb, pp::kScanThreads + 32, 0, s>>>(
+      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), lg_per, npow, block_val, ticket,
+      static_cast<fr *>(d_y));
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();
   return PP_OK;
@@ -784,7 +953,7 @@ extern "C" int pp_eval_noalloc(const void *d_poly, uint64_t n, const void *d_x, 
   // every block summary read by k_eval_final is written by k_affine_local in
   // the same call, so nothing in the array has to be cleared first
   fr *ba = scratch, *bb = scratch + pp::kEvalNoAllocMaxBlocks;
-  pp::k_affine_local<<<g.blocks, pp::kScanThreads, 0, s>>>(
+  pp::k_affine_local<<<g.blocks, pp::kScanThreads + 32, 0, s>>>(
       static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), 0, nullptr, nullptr, ba, bb);
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();

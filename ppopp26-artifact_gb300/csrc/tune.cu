@@ -202,3 +202,129 @@ extern "C" int pp_tune_load(const char *path) {
   }
   return PP_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Integer-pipe microbenchmark: the measured denominators of the integer
+// roofline.  Every launch fills each SM with 2048 threads; each thread runs
+// kIntChains independent dependency chains of one instruction kind, so the
+// pipe, not latency, bounds it.  Rates are lane operations per second (one
+// warp instruction = 32 lane operations).
+// ---------------------------------------------------------------------------
+namespace pp {
+namespace {
+
+constexpr int kIntChains = 8;
+constexpr int kIntIters = 4096;
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_int_rate(uint32_t seed, uint32_t *sink) {
+  uint32_t acc[kIntChains];
+  uint64_t wide[kIntChains];
+  const uint32_t a = seed ^ (threadIdx.x * 0x9e3779b9u), b = seed + blockIdx.x;
+#pragma unroll
+  for (int k = 0; k < kIntChains; ++k) {
+    acc[k] = a + k;
+    wide[k] = ((uint64_t)b << 32) ^ k;
+  }
+#pragma unroll 1
+  for (int it = 0; it < kIntIters; ++it) {
+#pragma unroll
+    for (int k = 0; k < kIntChains; ++k) {
+      if (KIND == 0) {
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(acc[k]) : "r"(a), "r"(b));
+      } else if (KIND == 1) {
+        asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(acc[k]) : "r"(a), "r"(b));
+      } else {
+        // 32 x 32 -> 64-bit product with a 64-bit addend: the row product of
+        // the Montgomery multiply
+        // the multiplicand is the accumulator's low word, so the product
+        // depends on the chain and cannot be hoisted out of the loop
+        asm volatile("{\n\t.reg .u32 l, h;\n\tmov.b64 {l, h}, %0;\n\tmad.wide.u32 %0, l, %1, %0;\n\t}"
+                     : "+l"(wide[k]) : "r"(a));
+      }
+    }
+  }
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kIntChains; ++k) s ^= acc[k] ^ (uint32_t)wide[k] ^ (uint32_t)(wide[k] >> 32);
+  if (s == 0x12345678u) sink[0] = s;  // keeps the chains live
+}
+
+// vals[i] = the Montgomery form of i + 1, i < n
+__global__ void k_fill_small(fr *vals, int n) {
+  if ((int)threadIdx.x >= n) return;
+  fr v = fr_one();
+  for (uint32_t k = 0; k < threadIdx.x; ++k) v = fr_add(v, fr_one());
+  st_fr(vals + threadIdx.x, v);
+}
+
+__global__ void __launch_bounds__(256) k_mm_rate(const fr *in, fr *sink, int iters) {
+  fr x = ld_fr(in + (threadIdx.x & 7)), y = ld_fr(in + 8 + (threadIdx.x & 7));
+  const fr w = ld_fr(in + 16);
+#pragma unroll 1
+  for (int it = 0; it < iters; ++it) {
+    x = fr_mul(x, w);
+    y = fr_mul(y, w);
+  }
+  if (fr_is_zero(x) && fr_is_zero(y)) st_fr(sink, x);  // keeps the chains live
+}
+
+}  // namespace
+}  // namespace pp
+
+// out[0]: mad.lo.u32, out[1]: mad.hi.u32, out[2]: mad.wide.u32 lane operations
+// per second; out[3]: Montgomery multiplies per second (two independent chains
+// per thread, the standalone rate of the field multiply).  Uses a 1 KiB
+// workspace; about 30 ms of GPU time.
+extern "C" int pp_measure_int_rates(double out[4]) {
+  if (!out) return PP_E_INVAL;
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  const int sms = pp::device_sm_count();
+  const uint32_t blocks = (uint32_t)sms * 8;
+  int st = PP_OK;
+  auto *ws = static_cast<uint32_t *>(pp::workspace_get(1024, nullptr, 9, &st));
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  PP_CUDA_TRY(cudaEventCreate(&e0));
+  PP_CUDA_TRY(cudaEventCreate(&e1));
+  const double lane_ops = (double)blocks * 256 * pp::kIntIters * pp::kIntChains;
+  for (int kind = 0; kind < 3 && st == PP_OK; ++kind) {
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
+      cudaEventRecord(e0, nullptr);
+      if (kind == 0) pp::k_int_rate<0><<<blocks, 256>>>(0x1234u + rep, ws);
+      else if (kind == 1) pp::k_int_rate<1><<<blocks, 256>>>(0x1234u + rep, ws);
+      else pp::k_int_rate<2><<<blocks, 256>>>(0x1234u + rep, ws);
+      PP_COUNT_LAUNCH();
+      cudaEventRecord(e1, nullptr);
+      if (cudaEventSynchronize(e1) != cudaSuccess) st = PP_E_CUDA;
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    out[kind] = lane_ops / (ms * 1e-3);
+  }
+  if (st == PP_OK) {
+    // field-multiply rate: inputs are 17 small Montgomery values
+    auto *vals = reinterpret_cast<pp::fr *>(ws + 64);
+    pp::k_fill_small<<<1, 32>>>(vals, 17);
+    PP_COUNT_LAUNCH();
+    const int iters = 256;
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, nullptr);
+      pp::k_mm_rate<<<blocks, 256>>>(vals, vals + 17, iters);
+      PP_COUNT_LAUNCH();
+      cudaEventRecord(e1, nullptr);
+      if (cudaEventSynchronize(e1) != cudaSuccess) st = PP_E_CUDA;
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    out[3] = (double)blocks * 256 * 2 * iters / (ms * 1e-3);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != PP_OK) {
+    cudaGetLastError();
+    pp::set_error("pp_measure_int_rates: a microbenchmark launch failed");
+  }
+  return st;
+}
