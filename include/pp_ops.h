@@ -112,6 +112,23 @@ int pp_ntt_host(const void *h_in, void *h_out, uint32_t lg_n, int inverse, void 
 int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda, uint32_t mode,
                 void *stream);
 
+/* Out-of-core transform: input, output and one intermediate buffer (all
+ * 32 * 2^lg_n bytes, page-locked host memory, three distinct buffers) stay in
+ * host memory.  Every pass reads its tiles from host memory and writes them
+ * back (NVLink-C2C on Grace hosts), whole 128-byte lines per warp access; the
+ * inter-pass twiddles come from two tables of about 2^(lg_n / 2) elements
+ * (w^i and w^(i 2^h), one extra multiply per element and pass), so device
+ * memory holds only those tables and the in-pass twiddles: under 5 MiB at
+ * 2^30 points.  The result equals pp_ntt bit for bit.  h_scratch is
+ * overwritten.  Asynchronous on the stream.  Replaces the reference's
+ * segmented out-of-core pipeline our_ntt (ntt.cu:979-1037), which streams
+ * chunks of 2^(lg_i + lg_k) elements through device buffers
+ * (run_first_ntt_pass :801, run_second_ntt_pass_async_scatter :861) and
+ * gathers and scatters them on the CPU; here the permutation is the tiles'
+ * own index arithmetic on the GPU. */
+int pp_ntt_out_of_core(const void *h_in, void *h_out, void *h_scratch, uint32_t lg_n, int inverse,
+                       void *stream);
+
 /* count transforms of page-locked host polynomials of 2^lg_n elements:
  * h_out[j] = NTT (or INTT) of h_in[j].  h_in[j] == h_out[j] is allowed; an
  * output must not overlap another polynomial's input.  Each polynomial is
@@ -257,6 +274,11 @@ typedef struct pp_server_config {
   uint32_t min_lg, max_lg;
   uint32_t lambda;       /* LDE blowup of every bundle */
   uint32_t max_queue;    /* 0 = unbounded; else pp_server_submit returns PP_E_BUSY when full */
+  /* 0 = no limit; else a bundle is admitted only while the estimated work of
+   * the running bundles plus its own stays at or below this many Montgomery
+   * multiplies (pp_bundle_work), or when nothing runs: large bundles then run
+   * nearly alone and small ones fill in beside them */
+  uint64_t max_inflight_mm;
 } pp_server_config;
 typedef struct pp_bundle {
   uint32_t lg_n;
@@ -280,6 +302,10 @@ typedef struct pp_server_stats {
   uint64_t completed, queued, budget_used, budget_peak, admitted_while_busy, max_concurrent;
   double p50_ms, p99_ms, bundles_per_s;
 } pp_server_stats;
+/* the algorithmic Montgomery multiplies of one bundle (the admission estimate):
+ * 3 LDEs of 2^lg_n coefficients onto 2^(lg_n+lambda) points, the grand
+ * product (16 per element), the division and 6 evaluations (1 per element each) */
+uint64_t pp_bundle_work(uint32_t lg_n, uint32_t lambda);
 int pp_server_create(const pp_server_config *cfg, void **server);
 int pp_server_submit(void *server, const pp_bundle *bundle, uint64_t *ticket);
 int pp_server_wait(void *server, uint64_t ticket, int timeout_ms, pp_bundle_result *result);
@@ -444,6 +470,8 @@ uint64_t pp_launch_count(void);
  * a diagnostic with no counterpart in the reference, which lets a caller check
  * that a call allocated nothing */
 uint64_t pp_device_alloc_count(void);
+/* bytes of those allocations (requested sizes, freed or not) */
+uint64_t pp_device_alloc_bytes(void);
 
 /* drop cached tables and workspaces of the current device (synchronises it) */
 int pp_release(void);

@@ -26,10 +26,18 @@ COMPAT_LIB = os.path.join(HERE, "libppcompat.so")
 COMPAT_DRIVER = os.path.join(HERE, "pp_compat_driver")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# Montgomery multiply formulation (csrc/fr.cuh); overridable for experiments
+# Montgomery multiply formulation (csrc/fr.cuh), the transform's twiddle
+# multiply (PP_NTT_MUL) and the pass kernels' blocks per SM (PP_NTT_MINB);
+# overridable for experiments
 MUL_VARIANT = os.environ.get("PP_MUL_VARIANT", "9")
+NTT_MUL = os.environ.get("PP_NTT_MUL", "")
+NTT_MINB = os.environ.get("PP_NTT_MINB", "")
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-DPP_MUL_VARIANT=" + MUL_VARIANT,
               "-I" + os.path.join(ROOT, "include")]
+if NTT_MUL:
+    NVCC_FLAGS.append("-DPP_NTT_MUL=" + NTT_MUL)
+if NTT_MINB:
+    NVCC_FLAGS.append("-DPP_NTT_MINB=" + NTT_MINB)
 
 
 def _nvcc() -> str:

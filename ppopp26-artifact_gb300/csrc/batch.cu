@@ -170,7 +170,7 @@ extern "C" int pp_batch_create(const pp_job *jobs, uint32_t count, void **plan_o
     ws_elems += gg[i].threads + gg[i].blocks;
   }
   size_t ws_bytes = pp::align_up(ws_elems * sizeof(fr), 256);
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(ws_bytes ? ws_bytes : 256);
   cudaError_t e = cudaMalloc(&p->d_mem, ws_bytes ? ws_bytes : 256);
   if (e != cudaSuccess) {
     pp::set_error("pp_batch_create: %zu bytes of workspace: %s", ws_bytes, cudaGetErrorString(e));
@@ -214,7 +214,7 @@ extern "C" int pp_batch_create(const pp_job *jobs, uint32_t count, void **plan_o
   desc_bytes += pp::align_up(gj.size() * sizeof(pp::GpBatchJob), 256) +
                 pp::align_up(gstart.size() * sizeof(uint32_t), 256);
   char *d_desc = nullptr;
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(desc_bytes ? desc_bytes : 256);
   e = cudaMalloc(reinterpret_cast<void **>(&d_desc), desc_bytes ? desc_bytes : 256);
   if (e != cudaSuccess) {
     cudaFree(p->d_mem);

@@ -63,13 +63,16 @@ __device__ __forceinline__ void st_fr(fr *p, const fr &v) {
 // One buffer per (device, stream, slot): work queued on one stream is ordered,
 // so calls on that stream may reuse it; different streams never share one.
 void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status);
+// frees every workspace of `stream` (call before destroying the stream)
+void workspace_release_stream(cudaStream_t stream);
 
 // counts kernel launches issued by this library (pp_launch_count)
 void count_launch();
 #define PP_COUNT_LAUNCH() ::pp::count_launch()
 // every device allocation this library requests (cudaMalloc, cudaMallocAsync,
-// cudaMallocFromPoolAsync) is counted; pp_device_alloc_count() reads the total
-void count_alloc();
-#define PP_COUNT_ALLOC() ::pp::count_alloc()
+// cudaMallocFromPoolAsync) is counted with its size; pp_device_alloc_count()
+// and pp_device_alloc_bytes() read the totals
+void count_alloc(size_t bytes);
+#define PP_COUNT_ALLOC(bytes) ::pp::count_alloc(bytes)
 
 }  // namespace pp

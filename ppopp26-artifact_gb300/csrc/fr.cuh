@@ -837,6 +837,7 @@ PP_HD void mul8_kara_rows(uint32_t r[16], const uint32_t a[8], const uint32_t b[
 
 // word-serial Montgomery reduction of t[0..16) with variant 9's rows; the
 // carry out of round i's top word (i + 8) is added at round i+1's top word
+template <bool LAZY = false>
 PP_HD fr mont_redc16_rows(uint32_t t[16]) {
   const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
   uint32_t hc = 0;
@@ -866,7 +867,7 @@ PP_HD fr mont_redc16_rows(uint32_t t[16]) {
   fr out;
 #pragma unroll
   for (int i = 0; i < 8; ++i) out.v[i] = t[8 + i];
-  fr_reduce_once(out.v);
+  if (!LAZY) fr_reduce_once(out.v);
   return out;
 }
 
@@ -926,6 +927,24 @@ PP_HD fr fr_mul_lazy(const fr &a, const fr &b) {
   fr c = a;
   fr_reduce_once(c.v);
   return fr_mul(c, b);
+#endif
+}
+
+// The transform's twiddle multiply: a < 2r, b < r (a twiddle), result < 2r.
+// PP_NTT_MUL selects its formulation (9: fr_mul_lazy's rows; 10: one
+// Karatsuba level for the product, 48 wide products instead of 64, then the
+// same row-wise reduction without the final subtraction: for a < 2r, b < r
+// the reduced value (a b + m r) / R < (2 r^2 + R r) / R < 2r).
+#ifndef PP_NTT_MUL
+#define PP_NTT_MUL 9
+#endif
+PP_HD fr fr_mul_twiddle(const fr &a, const fr &b) {
+#if PP_NTT_MUL == 10
+  uint32_t t[16];
+  mul8_kara_rows(t, a.v, b.v);
+  return mont_redc16_rows<true>(t);
+#else
+  return fr_mul_lazy(a, b);
 #endif
 }
 

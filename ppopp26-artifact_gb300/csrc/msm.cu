@@ -815,7 +815,7 @@ extern "C" int pp_msm_g1_bases_create(const void *d_points, uint64_t n, uint32_t
   int dev = 0;
   PP_CUDA_TRY(cudaGetDevice(&dev));
   g1a *table = nullptr;
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(W * n * sizeof(g1a));
   if (cudaMalloc(&table, W * n * sizeof(g1a)) != cudaSuccess) {
     cudaGetLastError();
     set_error("pp_msm_g1_bases_create: cannot allocate %llu bytes of window tables",
@@ -823,7 +823,7 @@ extern "C" int pp_msm_g1_bases_create(const void *d_points, uint64_t n, uint32_t
     return PP_E_NOMEM;
   }
   g1x *tmp = nullptr;
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(n * sizeof(g1x));
   if (cudaMallocAsync(&tmp, n * sizeof(g1x), s) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(table);

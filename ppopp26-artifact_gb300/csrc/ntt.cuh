@@ -15,6 +15,9 @@ struct PassArgs {
   fr *out;
   const fr *tw_inner;  // w_R^e, e < R
   const fr *tw_layer;  // w_{R S}^(c k) at [k][c], or null
+  // split layer twiddles (when tw_layer is null): w_{R S}^e =
+  // tw_hi[e >> tw_lgh] * tw_lo[e mod 2^tw_lgh], e = c k, or null
+  const fr *tw_lo, *tw_hi;
   const fr *diag;      // first pass, NTT_IN_DIAG
   fr post_scale;
   uint64_t n_valid;
@@ -22,6 +25,7 @@ struct PassArgs {
   uint32_t first, last, has_post_scale, in_kind, spread;
   uint32_t unit_in, unit_out;  // move 16-byte halves (host-memory input / output)
   uint32_t zero_lg;  // first pass: rows >= R >> zero_lg of every tile are zero (padding)
+  uint32_t tw_lgh;   // split layer twiddles: bits of the low table
   uint32_t P;
   uint32_t lgRp[4];
 };
@@ -49,6 +53,13 @@ struct NttInputDesc {
   bool in_host = false;
   bool out_host = false;
 };
+
+// The transform of 2^lg_m points with every pass reading and writing
+// page-locked host memory (h_in -> h_out, intermediates in h_scratch, all
+// three distinct) and the layer twiddles taken from split tables, so device
+// memory holds only tables of O(2^(lg_m / 2)) elements whatever lg_m is.
+int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m, bool inverse,
+                        cudaStream_t stream);
 
 // Runs the transform of 2^lg_m points: d_in -> d_out (may alias), on stream.
 // Returns a PP_* status.  Tables are built and cached on first use per device.

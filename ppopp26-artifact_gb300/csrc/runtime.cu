@@ -15,6 +15,7 @@ namespace {
 thread_local char t_err[512] = "";
 std::atomic<uint64_t> g_launches{0};
 std::atomic<uint64_t> g_allocs{0};
+std::atomic<uint64_t> g_alloc_bytes{0};
 
 struct WsKey {
   int dev;
@@ -41,7 +42,10 @@ void set_error(const char *fmt, ...) {
 const char *last_error() { return t_err; }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
-void count_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
+void count_alloc(size_t bytes) {
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
+  g_alloc_bytes.fetch_add(bytes, std::memory_order_relaxed);
+}
 
 int device_sm_count() {
   static int cached[64] = {0};
@@ -76,7 +80,7 @@ void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status) {
     b.ptr = nullptr;
     b.bytes = 0;
   }
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(bytes);
   cudaError_t e = cudaMalloc(&b.ptr, bytes);
   if (e != cudaSuccess) {
     b.ptr = nullptr;
@@ -88,6 +92,21 @@ void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status) {
   b.bytes = bytes;
   *status = PP_OK;
   return b.ptr;
+}
+
+// frees the workspaces of one stream (before the stream is destroyed); a
+// later stream may reuse the handle value, so stale entries must not stay
+void workspace_release_stream(cudaStream_t stream) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  for (auto it = g_ws.begin(); it != g_ws.end();) {
+    if (it->first.stream == stream) {
+      cudaStreamSynchronize(stream);
+      cudaFree(it->second.ptr);
+      it = g_ws.erase(it);
+    } else {
+      ++it;
+    }
+  }
 }
 
 int release_all() {
@@ -126,6 +145,8 @@ const char *pp_version(void) { return "ppfr 0.1 (sm_103a)"; }
 uint64_t pp_launch_count(void) { return pp::g_launches.load(); }
 
 uint64_t pp_device_alloc_count(void) { return pp::g_allocs.load(); }
+
+uint64_t pp_device_alloc_bytes(void) { return pp::g_alloc_bytes.load(); }
 
 int pp_release(void) { return pp::release_all(); }
 

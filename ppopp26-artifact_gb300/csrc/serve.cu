@@ -7,8 +7,9 @@
 //   one division by (X + c) (the quotient of an opening),
 //   6 evaluations (the 3 wires and 3 sigmas at 6 points).
 // A scheduler thread owns `slots` CUDA streams.  Submitted bundles wait in a
-// FIFO queue; whenever a slot is free and the bundle's device memory fits in
-// the HBM budget, the bundle is admitted: its buffers come from a stream-
+// FIFO queue; whenever a slot is free, the bundle's device memory fits in the
+// HBM budget and (with max_inflight_mm) the estimated work of the running
+// bundles leaves room for it, the bundle is admitted: its buffers come from a stream-
 // ordered memory pool, its inputs are generated on the device from its seed
 // or copied from pinned host memory, and its kernels are queued on the
 // slot's stream, so bundles admitted while others run overlap on the GPU.
@@ -48,6 +49,7 @@ struct Bundle {
   double t_submit = 0, t_start = 0, t_done = 0;
   int slot = -1;
   size_t bytes = 0;
+  uint64_t work = 0;    // pp_bundle_work
   void *mem = nullptr;  // one allocation: inputs, params, results
   cudaEvent_t done_ev = nullptr;
   // views into mem
@@ -76,6 +78,7 @@ struct Server {
   std::map<uint64_t, Bundle> bundles;
   uint64_t next_ticket = 1;
   size_t budget_used = 0, budget_peak = 0;
+  uint64_t inflight_work = 0;  // estimated multiplies of the running bundles
   std::atomic<bool> stop{false};
   std::thread worker;
   std::vector<double> latencies;
@@ -91,7 +94,7 @@ int launch_bundle(Server *S, Bundle &b) {
   cudaStream_t s = S->streams[b.slot];
   const uint32_t lg = b.req.lg_n, lam = b.req.lambda;
   const size_t n = size_t{1} << lg;
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(b.bytes);
   cudaError_t e = cudaMallocFromPoolAsync(&b.mem, b.bytes, S->pool, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -156,6 +159,7 @@ void worker_loop(Server *S) {
       }
       b.state = Bundle::DONE;
       S->slot_owner[sl] = 0;
+      S->inflight_work -= b.work;
       S->latencies.push_back(b.t_done - b.t_submit);
       S->last_done = b.t_done;
       ++S->completed;
@@ -176,14 +180,17 @@ void worker_loop(Server *S) {
         continue;
       }
       if (S->budget_used + b.bytes > S->cfg.budget_bytes) break;
-      S->queue.pop_front();
       size_t busy = 0;
       for (auto o : S->slot_owner) busy += o != 0;
+      // the work cap holds the head back while others run (never when idle)
+      if (busy && S->cfg.max_inflight_mm && S->inflight_work + b.work > S->cfg.max_inflight_mm) break;
+      S->queue.pop_front();
       if (busy) ++S->admitted_while_busy;
       S->max_concurrent = std::max<uint64_t>(S->max_concurrent, busy + 1);
       b.slot = free_slot;
       b.t_start = now_ms();
       S->budget_used += b.bytes;
+      S->inflight_work += b.work;
       S->budget_peak = std::max(S->budget_peak, S->budget_used);
       const int st = launch_bundle(S, b);
       if (st) {
@@ -193,6 +200,7 @@ void worker_loop(Server *S) {
         if (b.mem) cudaFreeAsync(b.mem, S->streams[b.slot]);
         b.mem = nullptr;
         S->budget_used -= b.bytes;
+        S->inflight_work -= b.work;
         b.status = st;
         b.state = Bundle::DONE;
         b.t_done = now_ms();
@@ -210,6 +218,12 @@ void worker_loop(Server *S) {
 }  // namespace pp
 
 using pp::Server;
+
+extern "C" uint64_t pp_bundle_work(uint32_t lg_n, uint32_t lambda) {
+  const uint64_t n = 1ull << lg_n, lg_m = lg_n + lambda;
+  const uint64_t lde = ((n << lambda) / 2) * lg_m + n;  // coset transform + the diagonal
+  return 3 * lde + 16 * n + n + 6 * n;
+}
 
 extern "C" int pp_server_create(const pp_server_config *cfg, void **srv) {
   if (!cfg || !srv || cfg->slots == 0 || cfg->slots > 64 || cfg->min_lg > cfg->max_lg ||
@@ -282,6 +296,7 @@ extern "C" int pp_server_submit(void *srv, const pp_bundle *req, uint64_t *ticke
   b.ticket = S->next_ticket++;
   b.req = *req;
   b.bytes = bytes;
+  b.work = pp_bundle_work(req->lg_n, req->lambda);
   b.t_submit = pp::now_ms();
   if (S->first_submit == 0) S->first_submit = b.t_submit;
   cudaError_t e = cudaEventCreateWithFlags(&b.done_ev, cudaEventDisableTiming);
@@ -408,7 +423,10 @@ extern "C" int pp_server_destroy(void *srv) {
     if (kv.second.mem) cudaFree(kv.second.mem);
     if (kv.second.done_ev) cudaEventDestroy(kv.second.done_ev);
   }
-  for (auto s : S->streams) cudaStreamDestroy(s);
+  for (auto s : S->streams) {
+    pp::workspace_release_stream(s);
+    cudaStreamDestroy(s);
+  }
   delete S;
   return PP_OK;
 }

@@ -148,6 +148,26 @@ extern "C" int pp_ntt_host(const void *h_in, void *h_out, uint32_t lg_n, int inv
                      lg_n, inverse != 0, in, (cudaStream_t)stream);
 }
 
+extern "C" int pp_ntt_out_of_core(const void *h_in, void *h_out, void *h_scratch, uint32_t lg_n,
+                                  int inverse, void *stream) {
+  if (lg_n > PP_MAX_LG_N) {
+    pp::set_error("pp_ntt_out_of_core: lg_n = %u exceeds %d", lg_n, PP_MAX_LG_N);
+    return PP_E_UNSUPPORTED;
+  }
+  const void *din = nullptr, *dout = nullptr, *dtmp = nullptr;
+  int st = host_view(h_in, "pp_ntt_out_of_core", "input", &din);
+  if (!st) st = host_view(h_out, "pp_ntt_out_of_core", "output", &dout);
+  if (!st) st = host_view(h_scratch, "pp_ntt_out_of_core", "scratch", &dtmp);
+  if (st) return st;
+  if (h_in == h_out || h_in == h_scratch || h_out == h_scratch) {
+    pp::set_error("pp_ntt_out_of_core: input, output and scratch must be three distinct buffers");
+    return PP_E_INVAL;
+  }
+  return pp::ntt_run_host_passes(static_cast<const fr *>(din), static_cast<fr *>(const_cast<void *>(dout)),
+                                 static_cast<fr *>(const_cast<void *>(dtmp)), lg_n, inverse != 0,
+                                 (cudaStream_t)stream);
+}
+
 extern "C" int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda,
                            uint32_t mode, void *stream) {
   if (lambda > 8 || mode > PP_LDE_SPREAD) {

@@ -81,9 +81,9 @@ extern "C" int pp_ntt_autotune(uint32_t lg_n, int reps, uint32_t *best_bits4, fl
   if (reps < 1) reps = 3;
   const uint64_t n = 1ull << lg_n;
   void *x = nullptr, *y = nullptr;
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(n * sizeof(pp::fr));
   PP_CUDA_TRY(cudaMalloc(&x, n * sizeof(pp::fr)));
-  PP_COUNT_ALLOC();
+  PP_COUNT_ALLOC(n * sizeof(pp::fr));
   cudaError_t e = cudaMalloc(&y, n * sizeof(pp::fr));
   if (e != cudaSuccess) {
     cudaFree(x);

@@ -177,6 +177,30 @@ def ntt_host_many(xs, inverse: bool = False, outs=None, stream=None):
     return outs
 
 
+def ntt_out_of_core(x, inverse: bool = False, out=None, scratch=None, stream=None):
+    """pp_ntt_out_of_core: page-locked host input, output and scratch (three
+    distinct buffers); device memory holds only small twiddle tables.
+    Asynchronous: synchronise the stream before reading out."""
+    lg = _lg(x.shape[0])
+    if out is None:
+        out = empty_pinned(x.shape[0])
+    if scratch is None:
+        scratch = empty_pinned(x.shape[0])
+    L = lib()
+    L.pp_ntt_out_of_core.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                     ctypes.c_int, ctypes.c_void_p]
+    L.pp_ntt_out_of_core.restype = ctypes.c_int
+    check(L.pp_ntt_out_of_core(_hptr(x), _hptr(out), _hptr(scratch), lg, int(inverse), _stream(stream)))
+    return out
+
+
+def device_alloc_bytes() -> int:
+    """Bytes of device memory this library has requested so far."""
+    L = lib()
+    L.pp_device_alloc_bytes.restype = ctypes.c_uint64
+    return int(L.pp_device_alloc_bytes())
+
+
 def lde_host(x, lam: int, mode: int = LDE_COEFFS, out=None, stream=None):
     """pp_lde_host: page-locked host input and output."""
     lg = _lg(x.shape[0])
@@ -634,7 +658,8 @@ class Batch:
 # ----------------------------------------------------------------- serving
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_uint64), ("slots", ctypes.c_uint32), ("min_lg", ctypes.c_uint32),
-                ("max_lg", ctypes.c_uint32), ("lam", ctypes.c_uint32), ("max_queue", ctypes.c_uint32)]
+                ("max_lg", ctypes.c_uint32), ("lam", ctypes.c_uint32), ("max_queue", ctypes.c_uint32),
+                ("max_inflight_mm", ctypes.c_uint64)]
 
 
 class _Bundle(ctypes.Structure):
@@ -667,10 +692,19 @@ def copy_to_host(dptr: int, n_elems: int):
     return out
 
 
+def bundle_work(lg_n: int, lam: int) -> int:
+    """pp_bundle_work: the algorithmic Montgomery multiplies of one bundle."""
+    L = lib()
+    L.pp_bundle_work.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    L.pp_bundle_work.restype = ctypes.c_uint64
+    return int(L.pp_bundle_work(lg_n, lam))
+
+
 class Server:
     """Continuous-batching server for prover-round bundles (pp_server_*)."""
 
-    def __init__(self, budget_bytes: int, slots: int, min_lg: int, max_lg: int, lam: int = 2, max_queue: int = 0):
+    def __init__(self, budget_bytes: int, slots: int, min_lg: int, max_lg: int, lam: int = 2, max_queue: int = 0,
+                 max_inflight_mm: int = 0):
         L = lib()
         L.pp_server_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
         L.pp_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
@@ -684,7 +718,7 @@ class Server:
                   "pp_server_cancel", "pp_server_get_stats", "pp_server_reset_stats", "pp_server_destroy"):
             getattr(L, n).restype = ctypes.c_int
         self.lam = lam
-        cfg = _ServerConfig(budget_bytes, slots, min_lg, max_lg, lam, max_queue)
+        cfg = _ServerConfig(budget_bytes, slots, min_lg, max_lg, lam, max_queue, max_inflight_mm)
         self._h = ctypes.c_void_p()
         check(L.pp_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
 

@@ -116,6 +116,14 @@ int main(int argc, char **argv) {
     if (!lazy_ok(ml, want) || std::memcmp(mc.v, want, 32)) {
       if (bad++ < 5) std::printf("lazy mul mismatch at %llu\n", (unsigned long long)i);
     }
+    // the transform's Karatsuba twiddle multiply (PP_NTT_MUL = 10), lazy
+    {
+      uint32_t t[16];
+      pp::mul8_kara_rows(t, xl.v, y.v);
+      if (!lazy_ok(pp::mont_redc16_rows<true>(t), want)) {
+        if (bad++ < 5) std::printf("lazy Karatsuba mul mismatch at %llu\n", (unsigned long long)i);
+      }
+    }
     or_fr_add(a + 4 * i, b + 4 * i, want);
     fr s = pp::fr_add(x, y);
     if (std::memcmp(s.v, want, 32) || !lazy_ok(pp::fr_add_lazy(xl, yl), want)) {

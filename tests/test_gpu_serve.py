@@ -106,6 +106,32 @@ def test_budget_admission_and_cancel(pp, cuda):
     srv.close()
 
 
+def test_work_cap_admission(pp, cuda):
+    """With the running work capped below two bundles' work, bundles run one
+    at a time (the cap never holds back a bundle when nothing runs), and the
+    results equal those of the uncapped server."""
+    P = pp.ppfr
+    lg = 14
+    one = P.bundle_work(lg, LAM)
+    assert one == 3 * ((4 << lg) // 2 * (lg + LAM) + (1 << lg)) + 23 * (1 << lg)
+    outs = []
+    for cap in (one + one // 2, 0):
+        srv = P.Server(budget_bytes=4 << 30, slots=4, min_lg=lg, max_lg=lg, lam=LAM, max_inflight_mm=cap)
+        ts = [srv.submit(lg, seed=9100 + i) for i in range(4)]
+        res = []
+        for t in ts:
+            r = srv.wait(t)
+            assert r.status == 0
+            res.append(fetch(P, r, lg))
+            srv.release(t)
+        st = srv.stats()
+        if cap:
+            assert st["max_concurrent"] == 1
+        outs.append(res)
+        srv.close()
+    assert all(same(a, b) for a, b in zip(*outs))
+
+
 def test_wait_is_bounded(pp, cuda):
     P = pp.ppfr
     srv = P.Server(budget_bytes=2 << 30, slots=1, min_lg=14, max_lg=14, lam=LAM)
