@@ -507,6 +507,16 @@ def host_resident_bench(pp, torch, rate, res):
             x, o = hin[:1 << lg], hout[:1 << (lg + lam)]
             name = "lde_host_2^%d_l%d" % (lg, lam)
             rate(name, lambda: ppfr.lde_host(x, lam, pp.LDE_COEFFS, out=o), 1 << lg, 3)
+    # out of core: every pass reads and writes host memory over the C2C link;
+    # the device holds only the twiddle tables
+    for lg in (24, 26):
+        n = 1 << lg
+        x, o, sc = hin[:n], hout[:n], hout[1 << 26:(1 << 26) + n]
+        name = "ntt_out_of_core_2^%d" % lg
+        rate(name, lambda: ppfr.ntt_out_of_core(x, out=o, scratch=sc), n, 3)
+        passes = -(-lg // 9)  # the plan splits lg into passes of at most 9 bits
+        gbs = 64 * passes * n / (res[name]["ms"] / 1e3) / 1e9
+        res[name].update({"passes": passes, "host_GB_per_s": round(gbs, 1)})
     del hin, hout
 
 

@@ -12,7 +12,9 @@ TEST/MEASUREMENT INFRASTRUCTURE.  Needs a GPU and the staged reference copy
   fixed 2^22 size).  Their ``../../input*.bin`` files are seeded random
   vectors of the right size;
 * the grand product, evaluation and division GPU calls and ``naive_gp`` /
-  ``naive_div`` (one host thread) at 2^20.
+  ``naive_div`` (one host thread) at 2^20, as the reference builds them
+  (``-O0`` host code) and from an ``-O2`` build of the same source
+  (``make -C oracle ref``).
 
     python oracle/ref_gpu_timings.py <out.json> [--quick]
 
@@ -135,6 +137,26 @@ def main() -> int:
             "naive_div": summary(floats(r"\[naive_div\] execution time: ([0-9.]+) ms", t)),
             "ours_div": summary(floats(r"\[ours_div\] execution time: ([0-9.]+) ms", t)),
         }
+    # the same naive_gp / naive_div from the -O2 build (oracle/Makefile ref)
+    L = O.ref_lib()
+    if L is not None:
+        import numpy as np
+        n = 1 << 20
+        a = O.random_fr(n, SEED + 120)
+        c = O.random_fr(1, SEED + 122)
+        out = np.empty_like(a)
+        t_gp, t_div = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            L.ref_naive_gp(20, a.ctypes.data, out.ctypes.data)
+            t_gp.append((time.perf_counter() - t0) * 1e3)
+            t0 = time.perf_counter()
+            L.ref_naive_div(20, a.ctypes.data, c.ctypes.data, out.ctypes.data)
+            t_div.append((time.perf_counter() - t0) * 1e3)
+        res["naive_O2_2p20"] = {"naive_gp": summary(t_gp), "naive_div": summary(t_div),
+                                "note": "ctypes call into the -O2 build; includes the harness's two 32 MiB copies"}
+    else:
+        res["naive_O2_2p20"] = {"unavailable": "oracle/_ref/libppref.so could not be built"}
     text = json.dumps(res, indent=1, sort_keys=True)
     with open(out_path, "w") as f:
         f.write(text + "\n")

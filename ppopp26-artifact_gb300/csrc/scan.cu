@@ -572,21 +572,23 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
 
 // ------------------------------------------------------------ evaluation
 // y = sum_i p_i x^i in one launch.
-//  * Thread t of the grid takes the K contiguous coefficients from t K and
-//    runs Horner over them: L_t = sum_{i<K} p_{tK+i} x^i.  K is chosen as for
-//    the other scans (scan_geom, two blocks per SM).
-//  * A block folds its 256 values pairwise, L_u + x^(K s) L_{u+s} for
-//    s = 1, 2, 4, ..., 128: V_b = sum_t L_t x^(K t), one multiply per fold.
-//  * The block that finishes last (a ticket counter) folds the block values
-//    the same way with the weights x^(T 2^j), T = 256 K, into y.
-// Every weight is (x^K)^(2^i) for some i, so a ninth warp of each block
-// computes x^K and then the squaring chain while the other eight run their
-// Horner chains: the weights of the block fold (i < 8) are ready by the time
-// the chains end, and the rest before the block's last barrier.
-// The fold's grouping of the sum does not change the value: field addition is
-// exact.
+//  * Thread t of block b takes the K contiguous coefficients from (256 b + t) K
+//    and runs Horner over them: L = sum_{i<K} p_{(256 b + t) K + i} x^i.  K is
+//    chosen as for the other scans (scan_geom, two blocks per SM).
+//  * Its term is L x^(K t) x^(256 K b).  Thread weights come from two 16-entry
+//    tables, x^(K a) and x^(16 K a) for a < 16 (x^(K t) = one product of an
+//    entry of each); the block's weight x^(256 K b) is one power.  Two helper
+//    warps compute the tables and that power while the other eight run their
+//    Horner chains.
+//  * Weighted terms are summed with field additions (warp shuffles, then the
+//    warps' sums); the block stores its sum times its weight, and the block
+//    that finishes last (a ticket counter) adds the block sums into y.
+// After the chains, a thread does two multiplies; every other step is an
+// addition.  A binary fold of the same terms (L_u + x^(K s) L_(u+s)) needs
+// eight dependent multiplies per block and as many more in the last block.
+// The sum's grouping does not change the value: field addition is exact.
 constexpr uint32_t kEvalBlocksPerSm = 2;
-constexpr uint32_t kEvalMaxPow = 48;
+constexpr uint32_t kEvalHelperWarps = 2;
 
 __device__ __forceinline__ fr ldcg_fr(const fr *p) {
   const uint4 *q = reinterpret_cast<const uint4 *>(p);
@@ -594,81 +596,85 @@ __device__ __forceinline__ fr ldcg_fr(const fr *p) {
   return fr{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w}};
 }
 
-// barrier of the 256 folding threads (warps 0-7); the power warp stays out
-__device__ __forceinline__ void fold_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
-// sv[0] := sum_u sv[u] w^u folded over 256 values, where the fold at
-// distance 2^j uses pw[first + j] = w^(2^j)
-__device__ __forceinline__ void fold256(fr *sv, const fr *pw, uint32_t first) {
-  const uint32_t tid = threadIdx.x;
-#pragma unroll 1
-  for (uint32_t j = 0; j < 8; ++j) {
-    if (tid < (kScanThreads >> (j + 1))) {
-      const uint32_t u = tid << (j + 1);
-      sv[u] = fr_add(sv[u], fr_mul(pw[first + j], sv[u + (1u << j)]));
-    }
-    fold_sync();
-  }
+__device__ __forceinline__ fr shfl_xor_fr(const fr &v, int o) {
+  fr r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = __shfl_xor_sync(0xffffffffu, v.v[i], o);
+  return r;
 }
 
-// g: K = g.k coefficients per thread; lg_per: each thread of the last block
-// folds 2^lg_per block values; the weights pw[i] = x^(K 2^i),
-// i < npow = 8 + lg_per + 8, are needed
-__global__ void __launch_bounds__(kScanThreads + 32)
-    k_eval_tree(const fr *__restrict__ p, ScanGeom g, const fr *__restrict__ xp, uint32_t lg_per,
-                uint32_t npow, fr *__restrict__ block_val, uint32_t *__restrict__ ticket,
-                fr *__restrict__ y) {
-  __shared__ fr pw[kEvalMaxPow];
-  __shared__ fr sv[kScanThreads];
+// sum over the 32 lanes of a warp (every lane gets it)
+__device__ __forceinline__ fr warp_sum_fr(fr v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fr_add(v, shfl_xor_fr(v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
+    k_eval_tree(const fr *__restrict__ p, ScanGeom g, const fr *__restrict__ xp,
+                fr *__restrict__ block_val, uint32_t *__restrict__ ticket, fr *__restrict__ y) {
+  __shared__ fr tab[32];  // tab[a] = x^(K a), tab[16 + a] = x^(16 K a), a < 16
+  __shared__ fr s_wb;     // x^(256 K b)
+  __shared__ fr s_warp[kScanThreads / 32];
   __shared__ uint32_t s_last;
-  const uint32_t tid = threadIdx.x;
+  constexpr uint32_t kHelpers = 32 * kEvalHelperWarps, kWarps = kScanThreads / 32;
+  // warps 0 and 1 are the helpers: the lowest warps of the block, which the
+  // warp schedulers tend to favour, so that their dependent chain of
+  // multiplies is not starved by the eight Horner warps
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t t = threadIdx.x - kHelpers, warp = t >> 5;  // Horner thread and warp
   const fr x = ld_fr(xp);
-  fr v = x;  // the power warp's running square
-  if (tid >= kScanThreads) {
-    // the power warp: one lane computes x^K and the weights of the block fold
-    if (tid == kScanThreads) {
-      v = fr_pow_u64(x, g.k);
-      pw[0] = v;
-      for (uint32_t i = 1; i < 8; ++i) {
-        v = fr_mul(v, v);
-        pw[i] = v;
-      }
-    }
+  fr L = fr_zero();
+  if (threadIdx.x < 32) {
+    // the tables: lane a < 16 raises x^K to a, lane 16 + a raises x^(16 K) to a
+    const fr v = fr_pow_u64(x, g.k);
+    fr u = v;
+#pragma unroll 1
+    for (int i = 0; i < 4; ++i) u = fr_sqr(u);
+    tab[lane] = fr_pow_u64(lane < 16 ? v : u, lane & 15);
+  } else if (threadIdx.x < kHelpers) {
+    // the block's weight: (x^(256 K))^b
+    fr v = fr_pow_u64(x, g.k);
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) v = fr_sqr(v);
+    v = fr_pow_u64(v, blockIdx.x);
+    if (lane == 0) s_wb = v;
   } else {
-    const uint64_t lo = ((uint64_t)blockIdx.x * kScanThreads + tid) * g.k;
-    fr L = fr_zero();
+    const uint64_t lo = ((uint64_t)blockIdx.x * kScanThreads + t) * g.k;
     if (lo < g.n) L = chunk_horner(p, lo, lo + g.k < g.n ? lo + g.k : g.n, x);
-    sv[tid] = L;
   }
-  __syncthreads();  // the block fold's weights and the chunk values are ready
-  if (tid == kScanThreads) {
-    // the rest of the chain, for the last block's fold, during the block fold
-    for (uint32_t i = 8; i < npow; ++i) {
-      v = fr_mul(v, v);
-      pw[i] = v;
-    }
-  }
-  if (tid < kScanThreads) fold256(sv, pw, 0);
-  if (tid == 0) {
-    st_fr(block_val + blockIdx.x, sv[0]);
-    __threadfence();
-    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();  // the tables, the block weight and the chunk values are ready
+  if (threadIdx.x >= kHelpers) {
+    const fr w = fr_mul(tab[t & 15], tab[16 + (t >> 4)]);  // x^(K t)
+    const fr sum = warp_sum_fr(fr_mul(L, w));
+    if (lane == 0) s_warp[warp] = sum;
   }
   __syncthreads();
-  if (!s_last || tid >= kScanThreads) return;
-  // last block: fold the gridDim.x block values, y = sum_b V_b x^(T b)
+  if (threadIdx.x < 32) {
+    fr v = warp_sum_fr(lane < kWarps ? s_warp[lane] : fr_zero());
+    if (lane == 0) {
+      st_fr(block_val + blockIdx.x, fr_mul(v, s_wb));
+      __threadfence();
+      s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!s_last) return;
+  // the last block: y = the sum of the gridDim.x weighted block sums
   __threadfence();
-  const uint32_t nb = gridDim.x;
-  const uint64_t b0 = (uint64_t)tid << lg_per;
-  fr V = fr_zero();
-  for (uint64_t b = b0 + (1ull << lg_per); b > b0; --b)
-    if (b - 1 < nb) V = fr_add(ldcg_fr(block_val + b - 1), fr_mul(pw[8], V));
-  sv[tid] = V;
-  fold_sync();
-  fold256(sv, pw, 8 + lg_per);
-  if (tid == 0) {
-    st_fr(y, sv[0]);
-    *ticket = 0;
+  if (threadIdx.x >= kHelpers) {
+    fr acc = fr_zero();
+    for (uint32_t b = t; b < gridDim.x; b += kScanThreads) acc = fr_add(acc, ldcg_fr(block_val + b));
+    acc = warp_sum_fr(acc);
+    if (lane == 0) s_warp[warp] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const fr v = warp_sum_fr(lane < kWarps ? s_warp[lane] : fr_zero());
+    if (lane == 0) {
+      st_fr(y, v);
+      *ticket = 0;
+    }
   }
 }
 
@@ -754,22 +760,15 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
   }
   const pp::ScanGeom g = pp::scan_geom(n, pp::kEvalBlocksPerSm);
   const uint32_t nb = g.blocks;
-  uint32_t lg_per = 0;
-  while (((uint64_t)pp::kScanThreads << lg_per) < nb) ++lg_per;
-  const uint32_t npow = 8 + lg_per + 8;
-  if (npow > pp::kEvalMaxPow) {
-    pp::set_error("pp_eval: %llu coefficients are too many", (unsigned long long)n);
-    return PP_E_UNSUPPORTED;
-  }
   int st = PP_OK;
-  // block values, then the ticket counter in its own 32-byte slot
+  // block sums, then the ticket counter in its own 32-byte slot
   char *ws = static_cast<char *>(pp::workspace_get((nb + 1) * sizeof(fr), s, 1, &st));
   if (st) return st;
   fr *block_val = reinterpret_cast<fr *>(ws);
   uint32_t *ticket = reinterpret_cast<uint32_t *>(ws + nb * sizeof(fr));
   PP_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
-  pp::k_eval_tree<<<nb, pp::kScanThreads + 32, 0, s>>>(
-      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), lg_per, npow, block_val, ticket,
+  pp::k_eval_tree<<<nb, pp::kScanThreads + 32 * pp::kEvalHelperWarps, 0, s>>>(
+      static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), block_val, ticket,
       static_cast<fr *>(d_y));
   PP_COUNT_LAUNCH();
   PP_LAUNCH_CHECK();

@@ -1,4 +1,8 @@
 // transform_api.cu -- C ABI of the transforms: NTT/INTT and the coset LDE.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "common.cuh"
 #include "ntt.cuh"
 
@@ -198,6 +202,48 @@ extern "C" int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_
 // the caller's stream wait for the last copy, so later work on that stream
 // (and a workspace reallocation, which synchronises it) is ordered after
 // every copy.
+namespace {
+// pp_ntt_host_many's copy streams and events for one (device, caller stream)
+struct HostManyCtx {
+  std::mutex mu;
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+  cudaEvent_t ev_in[3] = {}, ev_cmp[3] = {}, ev_out[3] = {};
+};
+std::mutex g_many_mu;
+std::map<std::pair<int, cudaStream_t>, HostManyCtx *> g_many;
+
+int host_many_ctx(cudaStream_t s, HostManyCtx **out) {
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_many_mu);
+  auto it = g_many.find({dev, s});
+  if (it != g_many.end()) {
+    *out = it->second;
+    return PP_OK;
+  }
+  auto *c = new HostManyCtx();
+  cudaError_t e = cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming);
+  for (int b = 0; b < 3 && e == cudaSuccess; ++b) {
+    e = cudaEventCreateWithFlags(&c->ev_in[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_cmp[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out[b], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    // a partly built context is kept out of the map and leaks its handles
+    cudaGetLastError();
+    pp::set_error("pp_ntt_host_many: stream or event creation failed: %s", cudaGetErrorString(e));
+    return PP_E_CUDA;
+  }
+  g_many[{dev, s}] = c;
+  *out = c;
+  return PP_OK;
+}
+}  // namespace
+
 extern "C" int pp_ntt_host_many(const void *const *h_in, void *const *h_out, uint32_t count,
                                 uint32_t lg_n, int inverse, void *stream) {
   if (lg_n > PP_MAX_LG_N) {
@@ -226,61 +272,47 @@ extern "C" int pp_ntt_host_many(const void *const *h_in, void *const *h_out, uin
   }
   int st = pp::ntt_prepare(lg_n, inverse != 0);
   if (st) return st;
-  // streams and events of this call; destroying them with work still queued
-  // is allowed (their resources go once that work completes)
-  cudaStream_t s_in = nullptr, s_out = nullptr;
-  cudaEvent_t ev_start = nullptr, ev_in[kBufs] = {}, ev_cmp[kBufs] = {}, ev_out[kBufs] = {};
-  auto cleanup = [&]() {
-    if (s_in) cudaStreamDestroy(s_in);
-    if (s_out) cudaStreamDestroy(s_out);
-    if (ev_start) cudaEventDestroy(ev_start);
-    for (int b = 0; b < kBufs; ++b) {
-      if (ev_in[b]) cudaEventDestroy(ev_in[b]);
-      if (ev_cmp[b]) cudaEventDestroy(ev_cmp[b]);
-      if (ev_out[b]) cudaEventDestroy(ev_out[b]);
-    }
-  };
-  cudaError_t e = cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming);
-  for (int b = 0; b < kBufs && e == cudaSuccess; ++b) {
-    e = cudaEventCreateWithFlags(&ev_in[b], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_cmp[b], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_out[b], cudaEventDisableTiming);
-  }
+  // the copy streams and events belong to the (device, caller stream) pair:
+  // created on its first call and reused, so a call creates nothing
+  HostManyCtx *c = nullptr;
+  st = host_many_ctx(s, &c);
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
   // the copy streams start after the work already queued on the caller's stream
-  if (e == cudaSuccess) e = cudaEventRecord(ev_start, s);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(s_in, ev_start, 0);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(s_out, ev_start, 0);
+  cudaError_t e = cudaEventRecord(c->ev_start, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_in, c->ev_start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_start, 0);
   pp::NttInputDesc desc;
   for (uint32_t j = 0; j < count && e == cudaSuccess && st == PP_OK; ++j) {
     const int b = (int)(j % kBufs);
-    if (j >= (uint32_t)kBufs) e = cudaStreamWaitEvent(s_in, ev_out[b], 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(buf[b], h_in[j], bytes, cudaMemcpyHostToDevice, s_in);
-    if (e == cudaSuccess) e = cudaEventRecord(ev_in[b], s_in);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_in[b], 0);
+    if (j >= (uint32_t)kBufs) e = cudaStreamWaitEvent(c->s_in, c->ev_out[b], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf[b], h_in[j], bytes, cudaMemcpyHostToDevice, c->s_in);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_in[b], c->s_in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_in[b], 0);
     if (e != cudaSuccess) break;
     st = pp::ntt_run(buf[b], buf[b], lg_n, inverse != 0, desc, s);
     if (st) break;
-    e = cudaEventRecord(ev_cmp[b], s);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s_out, ev_cmp[b], 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h_out[j], buf[b], bytes, cudaMemcpyDeviceToHost, s_out);
-    if (e == cudaSuccess) e = cudaEventRecord(ev_out[b], s_out);
+    e = cudaEventRecord(c->ev_cmp[b], s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_cmp[b], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_out[j], buf[b], bytes, cudaMemcpyDeviceToHost, c->s_out);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_out[b], c->s_out);
+  }
+  if (st || e != cudaSuccess) {
+    // copies already queued may still read h_in or write h_out: finish them
+    // before the caller can free those buffers on seeing the error
+    cudaStreamSynchronize(c->s_in);
+    cudaStreamSynchronize(c->s_out);
+    cudaGetLastError();
+    if (st) return st;
+    pp::set_error("pp_ntt_host_many: %s", cudaGetErrorString(e));
+    return PP_E_CUDA;
   }
   // the caller's stream waits for the last device-to-host copy (the copies
   // run in order on one stream, so that one covers them all)
-  cudaError_t e2 = cudaSuccess;
-  if (ev_start) {
-    cudaEvent_t done = nullptr;
-    e2 = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
-    if (e2 == cudaSuccess && s_out) e2 = cudaEventRecord(done, s_out);
-    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, done, 0);
-    if (done) cudaEventDestroy(done);
-  }
-  cleanup();
-  if (st) return st;
-  if (e != cudaSuccess || e2 != cudaSuccess) {
-    pp::set_error("pp_ntt_host_many: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+  e = cudaEventRecord(c->ev_done, c->s_out);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_done, 0);
+  if (e != cudaSuccess) {
+    pp::set_error("pp_ntt_host_many: %s", cudaGetErrorString(e));
     cudaGetLastError();
     return PP_E_CUDA;
   }
