@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
 // y = sum_i p_i x^i in one launch.
 //  * Thread t of block b takes the K contiguous coefficients from (256 b + t) K
 //    and runs Horner over them: L = sum_{i<K} p_{(256 b + t) K + i} x^i.  K is
-//    chosen as for the other scans (scan_geom, two blocks per SM).
+//    chosen as for the other scans (scan_geom; blocks per SM below).
 //  * Its term is L x^(K t) x^(256 K b).  Thread weights come from two 16-entry
 //    tables, x^(K a) and x^(16 K a) for a < 16 (x^(K t) = one product of an
 //    entry of each); the block's weight x^(256 K b) is one power.  Two helper
@@ -587,7 +587,13 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
 // addition.  A binary fold of the same terms (L_u + x^(K s) L_(u+s)) needs
 // eight dependent multiplies per block and as many more in the last block.
 // The sum's grouping does not change the value: field addition is exact.
-constexpr uint32_t kEvalBlocksPerSm = 2;
+// Blocks per SM: 1 up to 2^21 coefficients, 2 above.  At 2^20 the helpers'
+// powers (a chain of about 25 dependent multiplies, slowed by the Horner warps
+// that share their SM) end after the chains, so fewer Horner warps per SM
+// finish the block sooner (41.8 against 46.1 us); at 2^22 the chains are the
+// longer part and two blocks per SM are as fast (106 against 108 us).
+constexpr uint32_t kEvalBlocksPerSmSmall = 1, kEvalBlocksPerSm = 2;
+constexpr uint64_t kEvalSmallMax = 1ull << 21;
 constexpr uint32_t kEvalHelperWarps = 2;
 
 __device__ __forceinline__ fr ldcg_fr(const fr *p) {
@@ -758,7 +764,8 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
     PP_LAUNCH_CHECK();
     return PP_OK;
   }
-  const pp::ScanGeom g = pp::scan_geom(n, pp::kEvalBlocksPerSm);
+  const pp::ScanGeom g =
+      pp::scan_geom(n, n <= pp::kEvalSmallMax ? pp::kEvalBlocksPerSmSmall : pp::kEvalBlocksPerSm);
   const uint32_t nb = g.blocks;
   int st = PP_OK;
   // block sums, then the ticket counter in its own 32-byte slot
