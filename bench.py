@@ -461,16 +461,19 @@ def secondary_ops(pp, torch, int_peak=None):
             res[name]["out_Melem_per_s"] = round(res[name]["Melem_per_s"] * (1 << lam), 2)
         del o
     del x
-    n = 1 << 20
-    p = pp.random_fr(n, 2)
+    # the scans at the reference's miss_ops sizes: 2^20 (the BASELINE
+    # config) and 2^22 (its shipped main)
     z = pp.random_fr(1, 3)
     y = ppfr.empty(1)
-    rate("gp_prefix_2^20", lambda: pp.gp_prefix_(p), n, 10)
-    int_frac("gp_prefix_2^20", n, 64 * n)
-    rate("eval_2^20", lambda: pp.evaluate(p, z, out=y), n, 10)
-    int_frac("eval_2^20", n, 32 * n)
-    rate("div_2^20", lambda: pp.div_xplusc_(p, z), n, 10)
-    int_frac("div_2^20", n, 64 * n)
+    for lg in (22, 20):
+        n = 1 << lg
+        p = pp.random_fr(n, 2)
+        rate("gp_prefix_2^%d" % lg, lambda: pp.gp_prefix_(p), n, 10)
+        int_frac("gp_prefix_2^%d" % lg, n, 64 * n)
+        rate("eval_2^%d" % lg, lambda: pp.evaluate(p, z, out=y), n, 10)
+        int_frac("eval_2^%d" % lg, n, 32 * n)
+        rate("div_2^%d" % lg, lambda: pp.div_xplusc_(p, z), n, 10)
+        int_frac("div_2^%d" % lg, n, 64 * n)
     w = [pp.random_fr(n, 10 + j) for j in range(3)]
     s = [pp.random_fr(n, 20 + j) for j in range(3)]
     params = pp.random_fr(5, 30)
@@ -517,6 +520,13 @@ def host_resident_bench(pp, torch, rate, res):
         passes = -(-lg // 9)  # the plan splits lg into passes of at most 9 bits
         gbs = 64 * passes * n / (res[name]["ms"] / 1e3) / 1e9
         res[name].update({"passes": passes, "host_GB_per_s": round(gbs, 1)})
+    # out-of-core LDE from coefficients, 2^24 -> 2^26 (lambda = 2)
+    lg, lam = 24, 2
+    m = 1 << (lg + lam)
+    x, o, sc = hin[:1 << lg], hout[:m], hout[m:2 * m]
+    name = "lde_out_of_core_2^24_l2"
+    rate(name, lambda: ppfr.lde_out_of_core(x, lam, pp.LDE_COEFFS, out=o, scratch=sc), 1 << lg, 3)
+    res[name]["out_Melem_per_s"] = round(m / (res[name]["ms"] / 1e3) / 1e6, 2)
     del hin, hout
 
 
@@ -758,12 +768,26 @@ def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22):
     b.capture()
     ms_graph = time_device(b.run, 10, 2, torch) / 10
     b.close()
+    # the same comparison for each kind of job alone (plan against loop)
+    by_kind = {}
+    for label, ks in (("ntt_intt", (P.JOB_NTT, P.JOB_INTT)), ("lde_l2", (P.JOB_LDE_COEFFS,)),
+                      ("gp", (P.JOB_GP,))):
+        sel = [i for i, j in enumerate(jobs) if j[0] in ks]
+        if not sel:
+            continue
+        sub = [loop[i] for i in sel]
+        ms_l = time_device(lambda: [f() for f in sub], 3, 1, torch) / 3
+        bk = P.Batch([jobs[i] for i in sel])
+        ms_b = time_device(bk.run, 5, 2, torch) / 5
+        bk.close()
+        by_kind[label] = {"jobs": len(sel), "loop_ms": round(ms_l, 3), "batch_ms": round(ms_b, 3)}
     return {"polys": count, "lg_range": [lg_lo, lg_hi], "input_elems": elems,
             "loop_ms": round(ms_loop, 3),
             "loop_graph_ms": round(ms_loop_graph, 3) if ms_loop_graph else None,
             "batch_ms": round(ms_batch, 3),
             "graph_ms": round(ms_graph, 3), "loop_launches": int(loop_launches),
             "batch_launches": info["launches"], "speedup_batch": round(ms_loop / ms_batch, 3),
+            "by_kind": by_kind,
             "speedup_graph": round(ms_loop / ms_graph, 3),
             "Melem_per_s_graph": round(elems / (ms_graph / 1e3) / 1e6, 1)}
 

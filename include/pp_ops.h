@@ -129,6 +129,18 @@ int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda, u
 int pp_ntt_out_of_core(const void *h_in, void *h_out, void *h_scratch, uint32_t lg_n, int inverse,
                        void *stream);
 
+/* The LDE of pp_lde (same modes and results, bit for bit) with page-locked
+ * host input (2^lg_n elements), output and scratch (2^(lg_n + lambda) each),
+ * three distinct buffers: every pass reads and writes host memory, and the
+ * coset factors come from split tables of about 2^(lg_n / 2) entries, so
+ * device memory does not grow with the polynomial.  PP_LDE_EVALS also uses
+ * the output or the scratch buffer for the INTT's coefficients.  h_scratch
+ * is overwritten.  Asynchronous on the stream.  Replaces the reference's
+ * segmented out-of-core LDE (lde.cu:1033-1265: run_first_lde_pass :1033,
+ * run_lde_stage_pass :1137, under our_lde :1267). */
+int pp_lde_out_of_core(const void *h_in, void *h_out, void *h_scratch, uint32_t lg_n,
+                       uint32_t lambda, uint32_t mode, void *stream);
+
 /* count transforms of page-locked host polynomials of 2^lg_n elements:
  * h_out[j] = NTT (or INTT) of h_in[j].  h_in[j] == h_out[j] is allowed; an
  * output must not overlap another polynomial's input.  Each polynomial is

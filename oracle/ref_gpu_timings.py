@@ -5,7 +5,9 @@ TEST/MEASUREMENT INFRASTRUCTURE.  Needs a GPU and the staged reference copy
 ``make -C oracle refgpu`` and runs, on seeded synthetic inputs:
 
 * ``Ntt::forward`` / ``Intt::forward`` (in HBM; CUDA events around the call,
-  with and without the output allocation the call makes) at 2^22, 2^24, 2^26;
+  with and without the output allocation the call makes) at 2^22, 2^24, 2^26,
+  and at 2^22, 2^24 from the as-shipped build (sm_75 code and compute_75 PTX,
+  which the GB300 compiles at load: ``make -C oracle refgpu_jit``);
 * the reference's own benchmark commands, unmodified, from its main functions:
   ``NTT --bench-split`` and ``--bench-baseline`` (ntt.cu:1471), ``LDE --bench``
   and ``--bench-naive`` (lde.cu:1808), and miss_ops' main (miss_ops.cu:88, its
@@ -72,7 +74,9 @@ def main() -> int:
     quick = "--quick" in sys.argv
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     subprocess.run(["make", "-s", "-C", HERE, "-j16", "refgpu"], check=True)
+    jit_ok = subprocess.run(["make", "-s", "-C", HERE, "-j16", "refgpu_jit"]).returncode == 0
     ntt, lde, ops = (os.path.join(GPU_DIR, b) for b in ("ref_ntt", "ref_lde", "ref_ops"))
+    ntt_jit = os.path.join(HERE, "_ref", "gpu_jit", "ref_ntt")
     res: dict = {"host": {"machine": platform.machine(), "nproc": os.cpu_count()},
                  "build": "reference sources, reference flags (-O0 -g host), device code sm_103a"}
     try:
@@ -93,6 +97,15 @@ def main() -> int:
         for lg in sizes:
             res["ntt_in_hbm"][lg] = refjson(run([ntt, "time", str(lg), "10",
                                                  os.path.join(tmp, "input.bin" if lg == 22 else f"input-{lg}.bin")]))
+        # the same from the as-shipped build (PTX compiled by the driver at load)
+        res["ntt_in_hbm_as_shipped"] = {}
+        for lg in (22, 24):
+            if not jit_ok:
+                res["ntt_in_hbm_as_shipped"] = {"unavailable": "make -C oracle refgpu_jit failed"}
+                break
+            res["ntt_in_hbm_as_shipped"][lg] = refjson(run([ntt_jit, "time", str(lg), "10",
+                                                           os.path.join(tmp, "input.bin" if lg == 22
+                                                                        else f"input-{lg}.bin")]))
         # the reference's own NTT benchmarks
         res["our_ntt"], res["standard4_ntt"] = {}, {}
         for lg in sizes:

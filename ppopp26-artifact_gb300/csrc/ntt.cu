@@ -228,7 +228,12 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
           v = (g & ((1ull << a.spread) - 1)) == 0 ? ldcs_fr(a.in + (g >> a.spread)) : fr_zero();
         } else if (g < a.n_valid) {
           v = ldcs_fr(a.in + g);
-          if (a.in_kind == NTT_IN_DIAG) v = fr_mul_twiddle(v, ldcs_fr(a.diag + g));
+          if (a.in_kind == NTT_IN_DIAG) {
+            const fr d = a.diag_hi ? fr_mul(ldg_fr(a.diag + (g & ((1ull << a.diag_lgh) - 1))),
+                                            ldg_fr(a.diag_hi + (g >> a.diag_lgh)))
+                                   : ldcs_fr(a.diag + g);
+            v = fr_mul_twiddle(v, d);
+          }
         } else {
           v = fr_zero();
         }
@@ -938,6 +943,8 @@ int describe_passes(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inv
   a.P = plan->P;
   for (uint32_t j = 0; j < plan->P; ++j) a.lgRp[j] = plan->lgR[j];
   a.diag = in.diag;
+  a.diag_hi = in.diag_hi;
+  a.diag_lgh = in.diag_lgh;
   a.n_valid = in.n_valid ? in.n_valid : N;
   a.in_kind = (uint32_t)in.kind;
   a.spread = in.spread;
@@ -1043,20 +1050,47 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
   return PP_OK;
 }
 
+int ntt_host_plan_passes(uint32_t lg_m, uint32_t *passes) {
+  if (lg_m <= 11) {
+    *passes = 1;
+    return PP_OK;
+  }
+  int dev = 0;
+  PP_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  Plan *plan = nullptr;
+  const int st = get_plan(dev, lg_m, false, &plan, false, true);
+  if (st) return st;
+  *passes = plan->P;
+  return PP_OK;
+}
+
 int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m, bool inverse,
                         cudaStream_t stream) {
+  return ntt_run_host_passes(h_in, h_out, h_scratch, lg_m, inverse, NttInputDesc(), stream);
+}
+
+int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m, bool inverse,
+                        const NttInputDesc &desc, cudaStream_t stream) {
+  NttInputDesc in = desc;
+  in.in_host = in.out_host = true;
   if (lg_m <= 11) {
-    // one pass (or the tiny kernel): host in, host out, no intermediate
-    NttInputDesc in;
-    in.in_host = in.out_host = true;
+    // one pass (or the tiny kernel): host in, host out, no intermediate; a
+    // diagonal here is a full table (at most 2^11 entries)
+    if (in.diag_hi) {
+      set_error("transform of 2^%u points: split diagonal tables are for more than 2^11 points", lg_m);
+      return PP_E_INVAL;
+    }
     return ntt_run(h_in, h_out, lg_m, inverse, in, stream);
   }
   if (lg_m > PP_MAX_LG_N) {
     set_error("transform of 2^%u points exceeds the supported 2^%d", lg_m, PP_MAX_LG_N);
     return PP_E_UNSUPPORTED;
   }
-  NttInputDesc in;
-  in.in_host = in.out_host = true;
+  if (in.kind == NTT_IN_DIAG && !in.diag_hi) {
+    set_error("transform of 2^%u points over host memory: the diagonal must be split", lg_m);
+    return PP_E_INVAL;
+  }
   std::vector<PassArgs> passes;
   std::vector<uint64_t> tiles;
   int st = describe_passes(h_in, h_out, h_scratch, lg_m, inverse, in, passes, tiles, false, true);

@@ -19,6 +19,9 @@ struct PassArgs {
   // tw_hi[e >> tw_lgh] * tw_lo[e mod 2^tw_lgh], e = c k, or null
   const fr *tw_lo, *tw_hi;
   const fr *diag;      // first pass, NTT_IN_DIAG
+  // split diagonal (when non-null): diag factor of element g is
+  // diag[g mod 2^diag_lgh] * diag_hi[g >> diag_lgh]
+  const fr *diag_hi;
   fr post_scale;
   uint64_t n_valid;
   uint32_t lgR, lgT, lgS, lgN;
@@ -26,6 +29,7 @@ struct PassArgs {
   uint32_t unit_in, unit_out;  // move 16-byte halves (host-memory input / output)
   uint32_t zero_lg;  // first pass: rows >= R >> zero_lg of every tile are zero (padding)
   uint32_t tw_lgh;   // split layer twiddles: bits of the low table
+  uint32_t diag_lgh; // split diagonal: bits of the low table
   uint32_t P;
   uint32_t lgRp[4];
 };
@@ -45,6 +49,11 @@ enum NttInput { NTT_IN_PLAIN = 0, NTT_IN_DIAG = 1, NTT_IN_SPREAD = 2 };
 struct NttInputDesc {
   int kind = NTT_IN_PLAIN;
   const fr *diag = nullptr;
+  // NTT_IN_DIAG with split tables: diag holds h^j (j < 2^diag_lgh) and
+  // diag_hi holds h^(j 2^diag_lgh), so the factor h^g costs one more multiply
+  // and O(2^(lg / 2)) table entries instead of 2^lg
+  const fr *diag_hi = nullptr;
+  uint32_t diag_lgh = 0;
   uint64_t n_valid = 0;  // 0 = all 2^lg_m
   uint32_t spread = 0;
   // the input / output is page-locked host memory: the first pass reads and
@@ -60,6 +69,14 @@ struct NttInputDesc {
 // memory holds only tables of O(2^(lg_m / 2)) elements whatever lg_m is.
 int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m, bool inverse,
                         cudaStream_t stream);
+// The same with an input side (NTT_IN_PLAIN with n_valid, NTT_IN_DIAG with
+// split tables (diag_hi) above 2^11 points, NTT_IN_SPREAD); the host flags of
+// `in` are ignored (both ends are host memory).
+int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m, bool inverse,
+                        const NttInputDesc &in, cudaStream_t stream);
+
+// Passes of the plan ntt_run_host_passes uses for 2^lg_m points (1 up to 2^11).
+int ntt_host_plan_passes(uint32_t lg_m, uint32_t *passes);
 
 // Runs the transform of 2^lg_m points: d_in -> d_out (may alias), on stream.
 // Returns a PP_* status.  Tables are built and cached on first use per device.

@@ -172,6 +172,95 @@ extern "C" int pp_ntt_out_of_core(const void *h_in, void *h_out, void *h_scratch
                                  (cudaStream_t)stream);
 }
 
+namespace {
+// dst[i] = src[i], 16-byte words; stream-ordered (a host-to-host
+// cudaMemcpyAsync may run on the CPU ahead of the stream's kernels)
+__global__ void k_copy16(uint4 *__restrict__ dst, const uint4 *__restrict__ src, uint64_t n16) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// the diagonal h^i, i < 2^lg_n, of an LDE's first pass: one table up to 2^11
+// points, else two of about 2^(lg_n / 2) entries (h^j, h^(j 2^k))
+int lde_diag(const fr &h, uint32_t lg_n, uint32_t L, pp::NttInputDesc *d) {
+  int st = PP_OK;
+  d->kind = pp::NTT_IN_DIAG;
+  d->n_valid = 1ull << lg_n;
+  if (L <= 11) {
+    d->diag = pp::pow_table(h, lg_n, &st);
+    return st;
+  }
+  const uint32_t k = (lg_n + 1) / 2;
+  d->diag = pp::pow_table(h, k, &st);
+  if (st) return st;
+  d->diag_hi = pp::pow_table(pp::host_pow(h, 1ull << k), lg_n - k, &st);
+  d->diag_lgh = k;
+  return st;
+}
+}  // namespace
+
+extern "C" int pp_lde_out_of_core(const void *h_in, void *h_out, void *h_scratch, uint32_t lg_n,
+                                  uint32_t lambda, uint32_t mode, void *stream) {
+  if (lambda > 8 || mode > PP_LDE_SPREAD) {
+    pp::set_error("pp_lde_out_of_core: lambda %u / mode %u not supported", lambda, mode);
+    return PP_E_INVAL;
+  }
+  const uint32_t L = lg_n + lambda;
+  if (L > PP_MAX_LG_N) {
+    pp::set_error("pp_lde_out_of_core: 2^(%u+%u) exceeds the supported size", lg_n, lambda);
+    return PP_E_UNSUPPORTED;
+  }
+  const void *din = nullptr, *dout = nullptr, *dtmp = nullptr;
+  int st = host_view(h_in, "pp_lde_out_of_core", "input", &din);
+  if (!st) st = host_view(h_out, "pp_lde_out_of_core", "output", &dout);
+  if (!st) st = host_view(h_scratch, "pp_lde_out_of_core", "scratch", &dtmp);
+  if (st) return st;
+  if (h_in == h_out || h_in == h_scratch || h_out == h_scratch) {
+    pp::set_error("pp_lde_out_of_core: input, output and scratch must be three distinct buffers");
+    return PP_E_INVAL;
+  }
+  const cudaStream_t s = (cudaStream_t)stream;
+  const fr *in = static_cast<const fr *>(din);
+  fr *out = static_cast<fr *>(const_cast<void *>(dout)), *tmp = static_cast<fr *>(const_cast<void *>(dtmp));
+  if (mode == PP_LDE_SPREAD) {
+    // the N-point transform into out[0, N), then 2^lambda - 1 copies of it
+    st = pp::ntt_run_host_passes(in, out, tmp, lg_n, false, s);
+    if (st || lambda == 0) return st;
+    const uint64_t n16 = 2ull << lg_n;  // 16-byte words of N elements
+    for (uint64_t r = 1; r < (1ull << lambda); ++r) {
+      k_copy16<<<pp::device_sm_count() * 4, 256, 0, s>>>(reinterpret_cast<uint4 *>(out) + r * n16,
+                                                          reinterpret_cast<const uint4 *>(out), n16);
+      PP_COUNT_LAUNCH();
+      PP_LAUNCH_CHECK();
+    }
+    return PP_OK;
+  }
+  pp::NttInputDesc desc;
+  if (mode == PP_LDE_COEFFS) {
+    // coefficient i scaled by (7^(2^lambda))^i
+    st = lde_diag(pp::host_pow(pp::host_mont_small(7), 1ull << lambda), lg_n, L, &desc);
+    if (st) return st;
+    return pp::ntt_run_host_passes(in, out, tmp, L, false, desc, s);
+  }
+  // evaluations: the INTT's coefficients go to the buffer the main
+  // transform's first pass does not write (pass j writes out or scratch
+  // alternately, ending in out), and the main transform reads them from there
+  uint32_t P = 1;
+  st = pp::ntt_host_plan_passes(L, &P);
+  if (st) return st;
+  fr *coef = tmp, *other = out;
+  if (P >= 2 && ((P - 2) & 1) == 0) {  // pass 1 writes scratch
+    coef = out;
+    other = tmp;
+  }
+  st = pp::ntt_run_host_passes(in, coef, other, lg_n, true, s);
+  if (st) return st;
+  st = lde_diag(pp::host_mont_small(7), lg_n, L, &desc);
+  if (st) return st;
+  return pp::ntt_run_host_passes(coef, out, tmp, L, false, desc, s);
+}
+
 extern "C" int pp_lde_host(const void *h_in, void *h_out, uint32_t lg_n, uint32_t lambda,
                            uint32_t mode, void *stream) {
   if (lambda > 8 || mode > PP_LDE_SPREAD) {

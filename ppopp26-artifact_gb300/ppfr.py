@@ -194,6 +194,23 @@ def ntt_out_of_core(x, inverse: bool = False, out=None, scratch=None, stream=Non
     return out
 
 
+def lde_out_of_core(x, lam: int, mode: int = LDE_COEFFS, out=None, scratch=None, stream=None):
+    """pp_lde_out_of_core: page-locked host input (2^lg), output and scratch
+    (2^(lg + lam) each), three distinct buffers.  Asynchronous: synchronise the
+    stream before reading out."""
+    lg = _lg(x.shape[0])
+    if out is None:
+        out = empty_pinned(x.shape[0] << lam)
+    if scratch is None:
+        scratch = empty_pinned(x.shape[0] << lam)
+    L = lib()
+    L.pp_lde_out_of_core.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
+    L.pp_lde_out_of_core.restype = ctypes.c_int
+    check(L.pp_lde_out_of_core(_hptr(x), _hptr(out), _hptr(scratch), lg, lam, mode, _stream(stream)))
+    return out
+
+
 def device_alloc_bytes() -> int:
     """Bytes of device memory this library has requested so far."""
     L = lib()
