@@ -485,9 +485,9 @@ def secondary_ops(pp, torch, int_peak=None):
     elementwise_bench(pp, torch, rate, res)
     constraint_bench(pp, torch, rate, res, peak)
     msm_bench(pp, torch, rate, res, peak)
-    res["batched"] = batched_bench(pp, torch)
+    res["batched"] = batched_bench(pp, torch, peak=peak)
     # the launch-bound regime: many small polynomials
-    res["batched_small"] = batched_bench(pp, torch, 1024, 8, 14)
+    res["batched_small"] = batched_bench(pp, torch, 1024, 8, 14, peak=peak)
     res["serving"] = serving_bench(pp, torch)
     return res
 
@@ -714,7 +714,7 @@ def msm_bench(pp, torch, rate, res, peak):
     bases.close()
 
 
-def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22):
+def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22, peak=None):
     """count polynomials, sizes log-uniform in 2^lg_lo..2^lg_hi (seeded), in
     the proportions 2/3 NTT and INTT, 1/4 lambda=2 LDEs, 1/12 grand products
     (96 polynomials of 2^12..2^22: 64 / 24 / 8).  Loop of single calls vs one
@@ -744,6 +744,19 @@ def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22):
         else:
             loop.append(lambda x=x, out=out: (out.copy_(x), P.gp_prefix_(out)))
     elems = sum(1 << lg for lg in lgs)
+    # algorithmic multiplies of the mix: NTT (N/2) lg N, INTT + N, lambda = 2
+    # LDE from coefficients N + (4N/2)(lg N + 2), grand product N
+    mm = 0
+    for k, lg in zip(kinds, lgs):
+        n = 1 << lg
+        if k == P.JOB_NTT:
+            mm += n // 2 * lg
+        elif k == P.JOB_INTT:
+            mm += n // 2 * lg + n
+        elif k == P.JOB_LDE_COEFFS:
+            mm += n + 2 * n * (lg + 2)
+        else:
+            mm += n
     l0 = P.launch_count()
     ms_loop = time_device(lambda: [f() for f in loop], 3, 1, torch) / 3
     loop_launches = (P.launch_count() - l0) // 4
@@ -788,6 +801,13 @@ def batched_bench(pp, torch, count=96, lg_lo=12, lg_hi=22):
             "graph_ms": round(ms_graph, 3), "loop_launches": int(loop_launches),
             "batch_launches": info["launches"], "speedup_batch": round(ms_loop / ms_batch, 3),
             "by_kind": by_kind,
+            "algorithmic_MM": mm,
+            # the mix's time at the measured mad.lo rate (256 instructions per
+            # multiply), and the largest speed-up over the graph-captured loop
+            # that this integer ceiling allows
+            "int_ceiling_ms": round(mm * INSTR_PER_MM / peak * 1e3, 3) if peak else None,
+            "max_speedup_vs_loop_graph": (round(ms_loop_graph / (mm * INSTR_PER_MM / peak * 1e3), 2)
+                                          if peak and ms_loop_graph else None),
             "speedup_graph": round(ms_loop / ms_graph, 3),
             "Melem_per_s_graph": round(elems / (ms_graph / 1e3) / 1e6, 1)}
 
