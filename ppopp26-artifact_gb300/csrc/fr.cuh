@@ -914,7 +914,62 @@ PP_HD fr fr_mul(const fr &a, const fr &b) {
 #endif
 }
 
-PP_HD fr fr_sqr(const fr &a) { return fr_mul(a, a); }
+// r[0..16) = a^2 for a < 2^255: the 28 cross products a_i a_j (i < j) in rows
+// of independent products (row i: a_i times a_(i+1..7), each row's top word
+// new), doubled, plus the 8 squares a_i^2 in one add-with-carry chain: 36 wide
+// products where a general product needs 64.
+PP_HD void sqr8_rows(uint32_t r[16], const uint32_t a[8]) {
+#pragma unroll
+  for (int k = 0; k < 16; ++k) r[k] = 0;
+#pragma unroll
+  for (int i = 0; i < 7; ++i) {
+    const int n = 7 - i;  // partners a[i + 1 .. 7] at words 2i + 1 .. i + 7
+    uint32_t lo[7], hi[7];
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      const uint64_t s = (uint64_t)a[i] * a[i + 1 + j] + r[2 * i + 1 + j];
+      lo[j] = (uint32_t)s;
+      hi[j] = (uint32_t)(s >> 32);
+    }
+    r[2 * i + 1] = lo[0];
+    if (n == 1) {
+      r[2 * i + 2] = hi[0];
+    } else {
+      r[2 * i + 2] = add_cc(lo[1], hi[0]);
+#pragma unroll
+      for (int j = 2; j < n; ++j) r[2 * i + 1 + j] = addc_cc(lo[j], hi[j - 1]);
+      r[i + 8] = addc(hi[n - 1], 0);
+    }
+  }
+  // 2 x (the cross products) < a^2 < 2^510: the shift loses no bit
+#pragma unroll
+  for (int k = 15; k > 0; --k) r[k] = (r[k] << 1) | (r[k - 1] >> 31);
+  r[0] <<= 1;
+  uint32_t sl[8], sh[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint64_t s = (uint64_t)a[i] * a[i];
+    sl[i] = (uint32_t)s;
+    sh[i] = (uint32_t)(s >> 32);
+  }
+  r[0] = add_cc(r[0], sl[0]);
+  r[1] = addc_cc(r[1], sh[0]);
+#pragma unroll
+  for (int i = 1; i < 7; ++i) {
+    r[2 * i] = addc_cc(r[2 * i], sl[i]);
+    r[2 * i + 1] = addc_cc(r[2 * i + 1], sh[i]);
+  }
+  r[14] = addc_cc(r[14], sl[7]);
+  r[15] = addc(r[15], sh[7]);
+}
+
+// a^2 for canonical a (a^2 < r 2^256, as the reduction needs): the square's
+// 36 wide products, then the row-form Montgomery reduction (48)
+PP_HD fr fr_sqr(const fr &a) {
+  uint32_t t[16];
+  sqr8_rows(t, a.v);
+  return mont_redc16_rows(t);
+}
 
 // ---- lazy arithmetic on [0, 2r) for the NTT's inner rounds: values stay
 // below 2r and are made canonical once, when the transform stores its

@@ -110,6 +110,15 @@ int main(int argc, char **argv) {
         std::memcmp(m12.v, want, 32) || std::memcmp(m13.v, want, 32)) {
       if (bad++ < 5) std::printf("mul mismatch at %llu\n", (unsigned long long)i);
     }
+    // the dedicated square against the oracle's product of a value with itself
+    {
+      uint64_t want_sq[4];
+      or_fr_mul(a + 4 * i, a + 4 * i, want_sq);
+      const fr sq = pp::fr_sqr(x);
+      if (std::memcmp(sq.v, want_sq, 32)) {
+        if (bad++ < 5) std::printf("square mismatch at %llu\n", (unsigned long long)i);
+      }
+    }
     // lazy operands: either representative below 2r
     const fr xl = (i & 1) ? plus_r(x) : x, yl = (i & 2) ? plus_r(y) : y;
     const fr ml = pp::fr_mul_lazy(xl, y), mc = pp::fr_mul_row9(xl, y);
