@@ -1061,6 +1061,111 @@ PP_HD fr fr_canon(const fr &a) {
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// Dot products with one reduction per group of terms (Horner's chunks).  A
+// sum of G products of canonical values is below G r^2, so it is accumulated
+// in 17 words without reducing each product, and one Montgomery reduction of
+// the 17-word sum (below G r / 2 + r after it) plus a few conditional
+// subtractions gives the canonical result: 64 wide products per term and one
+// reduction per group, where a multiply per term costs 112.
+// ---------------------------------------------------------------------------
+// r[0..16) = a * b, rows of independent products + one add chain per row
+PP_HD void mul8_rows(uint32_t r[16], const uint32_t a[8], const uint32_t b[8]) {
+#pragma unroll
+  for (int k = 0; k < 16; ++k) r[k] = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint32_t lo[8], hi[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint64_t s = (uint64_t)a[i] * b[j] + r[i + j];
+      lo[j] = (uint32_t)s;
+      hi[j] = (uint32_t)(s >> 32);
+    }
+    r[i] = lo[0];
+    r[i + 1] = add_cc(lo[1], hi[0]);
+#pragma unroll
+    for (int j = 2; j < 8; ++j) r[i + j] = addc_cc(lo[j], hi[j - 1]);
+    r[i + 8] = addc(hi[7], 0);
+  }
+}
+
+// acc[0..17) += a * b
+PP_HD void fr_mac17(uint32_t acc[17], const fr &a, const fr &b) {
+  uint32_t p[16];
+  mul8_rows(p, a.v, b.v);
+  acc[0] = add_cc(acc[0], p[0]);
+#pragma unroll
+  for (int k = 1; k < 16; ++k) acc[k] = addc_cc(acc[k], p[k]);
+  acc[16] = addc(acc[16], 0);
+}
+
+// x - k r if x >= k r (x: 9 words)
+PP_HD void sub_if_ge9(uint32_t x[9], const uint32_t kr[9]) {
+  uint32_t t[9];
+  t[0] = sub_cc(x[0], kr[0]);
+#pragma unroll
+  for (int i = 1; i < 9; ++i) t[i] = subc_cc(x[i], kr[i]);
+  const uint32_t borrow = subc(0, 0);  // 0xffffffff if x < k r
+#pragma unroll
+  for (int i = 0; i < 9; ++i) x[i] = borrow ? x[i] : t[i];
+}
+
+// acc * 2^-256 mod r, canonical, for acc < 2^543 whose reduction is below
+// 16 r (a sum of at most 16 products of canonical values: acc < 16 r^2, so
+// the reduced value is below 16 r^2 / 2^256 + r < 8.3 r)
+PP_HD fr fr_redc17(uint32_t t[17]) {
+  const uint32_t r[8] = {PP_R0, PP_R1, PP_R2, PP_R3, PP_R4, PP_R5, PP_R6, PP_R7};
+  uint32_t hc = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    // round i: t += m r 2^(32 i) with m = -t[i] (r = 1 mod 2^32), as
+    // mont_redc16_rows; the carry out of word i + 8 rides into round i + 1
+    const uint32_t t0 = t[i];
+    const uint32_t m = 0u - t0;
+    uint32_t lo[8], hi[8];
+#pragma unroll
+    for (int j = 2; j < 8; ++j) {
+      const uint64_t s = (uint64_t)m * r[j] + t[i + j];
+      lo[j] = (uint32_t)s;
+      hi[j] = (uint32_t)(s >> 32);
+    }
+    (void)sub_cc(0, m);
+    const uint32_t h1 = subc(m, 0);
+    (void)add_cc(t0, 0xffffffffu);
+    t[i + 1] = addc_cc(t[i + 1], t0);
+    t[i + 2] = addc_cc(lo[2], h1);
+#pragma unroll
+    for (int j = 3; j < 8; ++j) t[i + j] = addc_cc(lo[j], hi[j - 1]);
+    t[i + 8] = addc_cc(t[i + 8], hi[7]);
+    const uint32_t c1 = addc(0, 0);
+    t[i + 8] = add_cc(t[i + 8], hc);
+    hc = addc(c1, 0);
+  }
+  t[16] += hc;  // the value t[8..17) is below 2^260: no carry leaves word 16
+  uint32_t x[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) x[i] = t[8 + i];
+  // k r for k = 8, 4, 2, 1
+  uint32_t kr[9];
+#pragma unroll
+  for (int sh = 3; sh >= 0; --sh) {
+    uint64_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      c += (uint64_t)r[i] << sh;
+      kr[i] = (uint32_t)c;
+      c >>= 32;
+    }
+    kr[8] = (uint32_t)c;
+    sub_if_ge9(x, kr);
+  }
+  fr out;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.v[i] = x[i];
+  return out;
+}
+
 // a^e for a 64-bit exponent (square and multiply, most significant bit first)
 PP_HD fr fr_pow_u64(const fr &a, uint64_t e) {
   fr acc = fr_one();

@@ -52,11 +52,43 @@ __device__ __forceinline__ fr chunk_product(const fr *p, uint64_t lo, uint64_t h
   return acc;
 }
 
-// Horner value sum_{lo <= i < hi} p[i] m^(i - lo) (hi > lo), from the top
-__device__ __forceinline__ fr chunk_horner(const fr *p, uint64_t lo, uint64_t hi, const fr &m) {
-  fr acc = ld_fr(p + hi - 1);
-  for (uint64_t i = hi - 1; i > lo; --i) acc = fr_add(ld_fr(p + i - 1), fr_mul(m, acc));
-  return acc;
+// sum_{lo <= i < hi} p[i] x^(i - lo) (hi > lo) from pw[k] = x^k, k <= 16, in
+// shared memory: groups of 16 coefficients are dot products with one
+// reduction each (fr_mac17 / fr_redc17), joined by Horner steps with x^16
+__device__ __forceinline__ fr chunk_dot(const fr *p, uint64_t lo, uint64_t hi, const fr *pw) {
+  const uint64_t ng = (hi - lo + 15) >> 4;
+  fr L = fr_zero();
+#pragma unroll 1
+  for (uint64_t g = ng; g-- > 0;) {
+    const uint64_t b = lo + (g << 4);
+    const uint32_t cnt = (uint32_t)(hi - b < 16 ? hi - b : 16);
+    uint32_t acc[17];
+#pragma unroll
+    for (int k = 0; k < 17; ++k) acc[k] = 0;
+#pragma unroll 1
+    for (uint32_t i = 0; i < cnt; ++i) fr_mac17(acc, ld_fr(p + b + i), pw[i]);
+    const fr S = fr_redc17(acc);
+    L = g + 1 == ng ? S : fr_add(fr_mul(L, pw[16]), S);
+  }
+  return L;
+}
+
+// pw[k] = x^k, k <= 16, by the 32 lanes of one warp: four doubling steps
+// (lanes 2^j < k <= 2^(j+1) take x^(k - 2^j) x^(2^j)); lanes 0..16 store
+__device__ __forceinline__ void warp_power_table17(const fr &x, fr *pw) {
+  const uint32_t lane = threadIdx.x & 31;
+  fr v = lane == 0 ? fr_one() : x;
+#pragma unroll 1
+  for (uint32_t h = 1; h <= 8; h <<= 1) {
+    fr lowv, hv;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      lowv.v[w] = __shfl_sync(0xffffffffu, v.v[w], (int)(lane >= h ? lane - h : 0));
+      hv.v[w] = __shfl_sync(0xffffffffu, v.v[w], (int)h);
+    }
+    if (lane > h && lane <= 2 * h) v = fr_mul(lowv, hv);
+  }
+  if (lane <= 16) pw[lane] = v;
 }
 
 // inclusive prefix product over a block of 256 threads (commutative);
@@ -486,7 +518,8 @@ __global__ void __launch_bounds__(kScanThreads)
 
 // per-thread exclusive suffix map (optional) and per-block map.  Launched
 // with kScanThreads + 32 threads: the extra warp computes m^K while the
-// others run their chunks' Horner chains, which do not need it.
+// others evaluate their chunks (chunk_dot, after the first warp's table of
+// m^0 .. m^16), which do not need it.
 __global__ void __launch_bounds__(kScanThreads + 32) k_affine_local(const fr *__restrict__ p, ScanGeom g,
                                                                      const fr *__restrict__ m_ptr,
                                                                      int negate_m, fr *thread_a,
@@ -494,6 +527,7 @@ __global__ void __launch_bounds__(kScanThreads + 32) k_affine_local(const fr *__
                                                                      fr *block_b) {
   __shared__ fr sa[kScanThreads], sb[kScanThreads];
   __shared__ fr s_mk;
+  __shared__ fr s_pw[17];  // m^k, k <= 16, for the chunks' dot products
   fr m = ld_fr(m_ptr);
   if (negate_m) m = fr_neg(m);
   if (threadIdx.x >= kScanThreads) {
@@ -501,10 +535,12 @@ __global__ void __launch_bounds__(kScanThreads + 32) k_affine_local(const fr *__
     __syncthreads();
     return;  // the scan below synchronises the other 256 threads by name
   }
+  if (threadIdx.x < 32) warp_power_table17(m, s_pw);
+  asm volatile("bar.sync 1, 256;" ::: "memory");
   const uint64_t gt = blockIdx.x * (uint64_t)kScanThreads + threadIdx.x;
   const uint64_t lo = gt * g.k < g.n ? gt * g.k : g.n;
   const uint64_t hi = lo + g.k < g.n ? lo + g.k : g.n;
-  const fr L = hi > lo ? chunk_horner(p, lo, hi, m) : fr_zero();
+  const fr L = hi > lo ? chunk_dot(p, lo, hi, s_pw) : fr_zero();
   __syncthreads();  // m^K ready
   fr a = L, b = hi - lo == g.k ? s_mk : hi > lo ? fr_pow_u64(m, hi - lo) : fr_one();
   block_affine_suffix<true>(a, b, sa, sb, thread_a != nullptr);
@@ -573,8 +609,11 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
 // ------------------------------------------------------------ evaluation
 // y = sum_i p_i x^i in one launch.
 //  * Thread t of block b takes the K contiguous coefficients from (256 b + t) K
-//    and runs Horner over them: L = sum_{i<K} p_{(256 b + t) K + i} x^i.  K is
-//    chosen as for the other scans (scan_geom; blocks per SM below).
+//    and evaluates them: L = sum_{i<K} p_{(256 b + t) K + i} x^i, as dot
+//    products of groups of 16 coefficients with x^0 .. x^15 (one reduction per
+//    group, chunk_dot) joined by Horner steps with x^16.  The first Horner warp
+//    builds x^0 .. x^16 first.  K is chosen as for the other scans (scan_geom;
+//    blocks per SM below).
 //  * Its term is L x^(K t) x^(256 K b).  Thread weights come from two 16-entry
 //    tables, x^(K a) and x^(16 K a) for a < 16 (x^(K t) = one product of an
 //    entry of each); the block's weight x^(256 K b) is one power.  Two helper
@@ -621,6 +660,7 @@ __global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
                 fr *__restrict__ block_val, uint32_t *__restrict__ ticket, fr *__restrict__ y) {
   __shared__ fr tab[32];  // tab[a] = x^(K a), tab[16 + a] = x^(16 K a), a < 16
   __shared__ fr s_wb;     // x^(256 K b)
+  __shared__ fr s_pw[17]; // x^k, k <= 16, for the Horner threads' dot products
   __shared__ fr s_warp[kScanThreads / 32];
   __shared__ uint32_t s_last;
   constexpr uint32_t kHelpers = 32 * kEvalHelperWarps, kWarps = kScanThreads / 32;
@@ -646,8 +686,12 @@ __global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
     v = fr_pow_u64(v, blockIdx.x);
     if (lane == 0) s_wb = v;
   } else {
+    // the first Horner warp builds x^0 .. x^16; the 256 Horner threads wait
+    // for it on a named barrier (the helper warps do not)
+    if (warp == 0) warp_power_table17(x, s_pw);
+    asm volatile("bar.sync 1, 256;" ::: "memory");
     const uint64_t lo = ((uint64_t)blockIdx.x * kScanThreads + t) * g.k;
-    if (lo < g.n) L = chunk_horner(p, lo, lo + g.k < g.n ? lo + g.k : g.n, x);
+    if (lo < g.n) L = chunk_dot(p, lo, lo + g.k < g.n ? lo + g.k : g.n, s_pw);
   }
   __syncthreads();  // the tables, the block weight and the chunk values are ready
   if (threadIdx.x >= kHelpers) {

@@ -94,6 +94,23 @@ int main(int argc, char **argv) {
     p[0] = ~0ull;
   }
   long bad = 0;
+  {
+    // the largest accumulation: 16 products of (r - 1)^2
+    uint32_t acc[17] = {0};
+    uint64_t want_dot[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 16; ++k) {
+      pp::fr_mac17(acc, load(rm1), load(rm1));
+      uint64_t prod[4], sum[4];
+      or_fr_mul(rm1, rm1, prod);
+      or_fr_add(want_dot, prod, sum);
+      std::memcpy(want_dot, sum, 32);
+    }
+    const fr got = pp::fr_redc17(acc);
+    if (std::memcmp(got.v, want_dot, 32)) {
+      bad++;
+      std::printf("dot product mismatch for 16 (r - 1)^2\n");
+    }
+  }
   for (uint64_t i = 0; i < n; ++i) {
     fr x = load(a + 4 * i), y = load(b + 4 * i);
     uint64_t want[4];
@@ -117,6 +134,24 @@ int main(int argc, char **argv) {
       const fr sq = pp::fr_sqr(x);
       if (std::memcmp(sq.v, want_sq, 32)) {
         if (bad++ < 5) std::printf("square mismatch at %llu\n", (unsigned long long)i);
+      }
+    }
+    // dot products of up to 16 terms with one reduction (fr_mac17 + fr_redc17)
+    if (i % 16 == 15) {
+      const int G = 1 + (int)((i / 16) % 16);
+      uint32_t acc[17] = {0};
+      uint64_t want_dot[4] = {0, 0, 0, 0};
+      for (int k = 0; k < G; ++k) {
+        const uint64_t *pa = a + 4 * (i - k), *pb = b + 4 * (i - k);
+        pp::fr_mac17(acc, load(pa), load(pb));
+        uint64_t prod[4], sum[4];
+        or_fr_mul(pa, pb, prod);
+        or_fr_add(want_dot, prod, sum);
+        std::memcpy(want_dot, sum, 32);
+      }
+      const fr got = pp::fr_redc17(acc);
+      if (std::memcmp(got.v, want_dot, 32)) {
+        if (bad++ < 5) std::printf("dot product mismatch at %llu (G = %d)\n", (unsigned long long)i, G);
       }
     }
     // lazy operands: either representative below 2r
