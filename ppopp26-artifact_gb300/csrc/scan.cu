@@ -65,8 +65,14 @@ __device__ __forceinline__ fr chunk_dot(const fr *p, uint64_t lo, uint64_t hi, c
     uint32_t acc[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) acc[k] = 0;
+    // each coefficient is loaded one term ahead of its multiply
+    fr cur = ld_fr(p + b);
 #pragma unroll 1
-    for (uint32_t i = 0; i < cnt; ++i) fr_mac17(acc, ld_fr(p + b + i), pw[i]);
+    for (uint32_t i = 0; i < cnt; ++i) {
+      const fr nxt = i + 1 < cnt ? ld_fr(p + b + i + 1) : cur;
+      fr_mac17(acc, cur, pw[i]);
+      cur = nxt;
+    }
     const fr S = fr_redc17(acc);
     L = g + 1 == ng ? S : fr_add(fr_mul(L, pw[16]), S);
   }
