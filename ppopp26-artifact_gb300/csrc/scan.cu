@@ -640,6 +640,10 @@ __global__ void __launch_bounds__(kScanThreads) k_eval_final(const fr *__restric
 constexpr uint32_t kEvalBlocksPerSmSmall = 1, kEvalBlocksPerSm = 2;
 constexpr uint64_t kEvalSmallMax = 1ull << 21;
 constexpr uint32_t kEvalHelperWarps = 2;
+// Horner threads per block (with the two helper warps on top).  128 per block
+// (fewer Horner warps beside the helpers, twice the coefficients per thread)
+// was slower: 37.9 against 35.5 us at 2^20, 85.2 against 82.8 us at 2^22.
+constexpr uint32_t kEvalHorner = 256;
 
 __device__ __forceinline__ fr ldcg_fr(const fr *p) {
   const uint4 *q = reinterpret_cast<const uint4 *>(p);
@@ -661,18 +665,18 @@ __device__ __forceinline__ fr warp_sum_fr(fr v) {
   return v;
 }
 
-__global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
+template <uint32_t HT>
+__global__ void __launch_bounds__(HT + 32 * kEvalHelperWarps)
     k_eval_tree(const fr *__restrict__ p, ScanGeom g, const fr *__restrict__ xp,
                 fr *__restrict__ block_val, uint32_t *__restrict__ ticket, fr *__restrict__ y) {
+  static_assert(HT % 32 == 0 && HT <= 256, "Horner threads: whole warps, at most 256");
+  constexpr uint32_t kHelpers = 32 * kEvalHelperWarps, kWarps = HT / 32;
   __shared__ fr tab[32];  // tab[a] = x^(K a), tab[16 + a] = x^(16 K a), a < 16
-  __shared__ fr s_wb;     // x^(256 K b)
+  __shared__ fr s_wb;     // x^(HT K b)
   __shared__ fr s_pw[17]; // x^k, k <= 16, for the Horner threads' dot products
-  __shared__ fr s_warp[kScanThreads / 32];
+  __shared__ fr s_warp[kWarps];
   __shared__ uint32_t s_last;
-  constexpr uint32_t kHelpers = 32 * kEvalHelperWarps, kWarps = kScanThreads / 32;
-  // warps 0 and 1 are the helpers: the lowest warps of the block, which the
-  // warp schedulers tend to favour, so that their dependent chain of
-  // multiplies is not starved by the eight Horner warps
+  // warps 0 and 1 are the helpers
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t t = threadIdx.x - kHelpers, warp = t >> 5;  // Horner thread and warp
   const fr x = ld_fr(xp);
@@ -685,18 +689,18 @@ __global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
     for (int i = 0; i < 4; ++i) u = fr_sqr(u);
     tab[lane] = fr_pow_u64(lane < 16 ? v : u, lane & 15);
   } else if (threadIdx.x < kHelpers) {
-    // the block's weight: (x^(256 K))^b
+    // the block's weight: (x^(HT K))^b
     fr v = fr_pow_u64(x, g.k);
 #pragma unroll 1
-    for (int i = 0; i < 8; ++i) v = fr_sqr(v);
+    for (uint32_t i = 1; i < HT; i <<= 1) v = fr_sqr(v);
     v = fr_pow_u64(v, blockIdx.x);
     if (lane == 0) s_wb = v;
   } else {
-    // the first Horner warp builds x^0 .. x^16; the 256 Horner threads wait
-    // for it on a named barrier (the helper warps do not)
+    // the first Horner warp builds x^0 .. x^16; the Horner threads wait for
+    // it on a named barrier (the helper warps do not)
     if (warp == 0) warp_power_table17(x, s_pw);
-    asm volatile("bar.sync 1, 256;" ::: "memory");
-    const uint64_t lo = ((uint64_t)blockIdx.x * kScanThreads + t) * g.k;
+    asm volatile("bar.sync 1, %0;" ::"n"(HT) : "memory");
+    const uint64_t lo = ((uint64_t)blockIdx.x * HT + t) * g.k;
     if (lo < g.n) L = chunk_dot(p, lo, lo + g.k < g.n ? lo + g.k : g.n, s_pw);
   }
   __syncthreads();  // the tables, the block weight and the chunk values are ready
@@ -720,7 +724,7 @@ __global__ void __launch_bounds__(kScanThreads + 32 * kEvalHelperWarps)
   __threadfence();
   if (threadIdx.x >= kHelpers) {
     fr acc = fr_zero();
-    for (uint32_t b = t; b < gridDim.x; b += kScanThreads) acc = fr_add(acc, ldcg_fr(block_val + b));
+    for (uint32_t b = t; b < gridDim.x; b += HT) acc = fr_add(acc, ldcg_fr(block_val + b));
     acc = warp_sum_fr(acc);
     if (lane == 0) s_warp[warp] = acc;
   }
@@ -814,8 +818,16 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
     PP_LAUNCH_CHECK();
     return PP_OK;
   }
-  const pp::ScanGeom g =
-      pp::scan_geom(n, n <= pp::kEvalSmallMax ? pp::kEvalBlocksPerSmSmall : pp::kEvalBlocksPerSm);
+  // scan_geom's rule with kEvalHorner threads per block
+  constexpr uint32_t HT = pp::kEvalHorner;
+  const uint32_t bps = n <= pp::kEvalSmallMax ? pp::kEvalBlocksPerSmSmall : pp::kEvalBlocksPerSm;
+  pp::ScanGeom g;
+  g.n = n;
+  const uint64_t target = (uint64_t)pp::device_sm_count() * bps * HT;
+  g.k = (n + target - 1) / target;
+  if (g.k < 4) g.k = 4;
+  g.threads = (n + g.k - 1) / g.k;
+  g.blocks = (uint32_t)((g.threads + HT - 1) / HT);
   const uint32_t nb = g.blocks;
   int st = PP_OK;
   // block sums, then the ticket counter in its own 32-byte slot
@@ -824,7 +836,7 @@ extern "C" int pp_eval(const void *d_poly, uint64_t n, const void *d_x, void *d_
   fr *block_val = reinterpret_cast<fr *>(ws);
   uint32_t *ticket = reinterpret_cast<uint32_t *>(ws + nb * sizeof(fr));
   PP_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
-  pp::k_eval_tree<<<nb, pp::kScanThreads + 32 * pp::kEvalHelperWarps, 0, s>>>(
+  pp::k_eval_tree<HT><<<nb, HT + 32 * pp::kEvalHelperWarps, 0, s>>>(
       static_cast<const fr *>(d_poly), g, static_cast<const fr *>(d_x), block_val, ticket,
       static_cast<fr *>(d_y));
   PP_COUNT_LAUNCH();
