@@ -28,6 +28,13 @@
 //   ref_ops div <lgN> <in> <c> <out>      poly_div_poly by (X + c) (in place)
 //   ref_ops time <lgN> <reps> <in> <x> <c> GPU ops (CUDA events) and the blst
 //                                         CPU baselines (wall clock, 1 thread)
+//   ref_ops msm <lgN> <reps> <points> <scalars> <out>
+//                                         multi_scalar_mult (PLONK/utils/function.cu:396-412)
+//                                         on 2^lgN affine points (96-byte x, y in
+//                                         Montgomery form) and plain 32-byte
+//                                         scalars; writes its Jacobian result
+//                                         (3 x 48 bytes); reps > 0 adds wall-clock
+//                                         times (its collection step runs on the host)
 //   ref_* refmain <args...>               the reference driver's own main
 // Every timing command prints one line "REFJSON {...}".
 #include <chrono>
@@ -289,6 +296,32 @@ static int unit_main(int argc, char** argv) {
     SyncedMemory out = poly_div_poly(in, c);
     check_cuda("poly_div_poly");
     write_all(argv[5], out.mutable_cpu_data(), n * 32);
+    return 0;
+  }
+  if (cmd == "msm" && argc == 7) {
+    const int lg = lg_arg(argv[2]);
+    const int reps = std::atoi(argv[3]);
+    const uint64_t n = uint64_t{1} << lg;
+    SyncedMemory pts(n * 96), sc(n * 32);
+    read_exact(argv[4], pts.mutable_cpu_data(), n * 96);
+    read_exact(argv[5], sc.mutable_cpu_data(), n * 32);
+    pts.mutable_gpu_data();
+    sc.mutable_gpu_data();
+    check_cuda("upload");
+    std::vector<double> t;
+    SyncedMemory res;
+    for (int r = -1; r < reps; ++r) {  // r = -1 is the warm-up (and the result kept)
+      const double ms = wall_ms([&] {
+        res = multi_scalar_mult(pts, sc);
+        cudaDeviceSynchronize();
+      });
+      if (r >= 0) t.push_back(ms);
+    }
+    check_cuda("multi_scalar_mult");
+    write_all(argv[6], res.mutable_cpu_data(), 3 * 48);
+    if (reps > 0)
+      std::printf("REFJSON {\"op\": \"msm\", \"lgN\": %d, \"multi_scalar_mult\": %s}\n", lg,
+                  stats_json(t).c_str());
     return 0;
   }
   if (cmd == "time" && argc == 7) {

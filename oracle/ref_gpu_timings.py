@@ -13,6 +13,10 @@ TEST/MEASUREMENT INFRASTRUCTURE.  Needs a GPU and the staged reference copy
   and ``--bench-naive`` (lde.cu:1808), and miss_ops' main (miss_ops.cu:88, its
   fixed 2^22 size).  Their ``../../input*.bin`` files are seeded random
   vectors of the right size;
+* ``multi_scalar_mult`` (PLONK/utils/function.cu:396-412; wall clock, since
+  its last step runs on the host) at 2^16 and 2^20 points: 1024 distinct
+  multiples of the generator, tiled, and seeded scalars, as ``bench.py`` times
+  ``pp_msm_g1``;
 * the grand product, evaluation and division GPU calls and ``naive_gp`` /
   ``naive_div`` (one host thread) at 2^20, as the reference builds them
   (``-O0`` host code) and from an ``-O2`` build of the same source
@@ -142,6 +146,16 @@ def main() -> int:
         O.random_fr(1, SEED + 121).tofile(fx)
         O.random_fr(1, SEED + 122).tofile(fc)
         res["miss_ops_2p20"] = refjson(run([ops, "time", "20", "10", fin, fx, fc]))
+        # G1 multi-scalar multiplication
+        import numpy as np
+        base = O.g1_mul_gen(O.random_fr(1024, SEED + 130))
+        fp, fs, fo = (os.path.join(tmp, f) for f in ("msm_p.bin", "msm_s.bin", "msm_o.bin"))
+        res["msm"] = {}
+        for lg in (16, 20):
+            n = 1 << lg
+            np.ascontiguousarray(np.tile(base, (n // 1024, 1)), dtype=np.uint64).tofile(fp)
+            O.random_fr(n, SEED + 131).tofile(fs)
+            res["msm"][lg] = refjson(run([ops, "msm", str(lg), "3", fp, fs, fo]))
         t = run([ops, "refmain"], cwd=wd, timeout=2400)
         res["miss_ops_main_2p22"] = {
             "naive_gp": summary(floats(r"\[naive_gp\] execution time: ([0-9.]+) ms", t)),
