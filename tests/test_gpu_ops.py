@@ -38,6 +38,27 @@ def test_div(pp, O, cuda, n):
     assert O.first_diff(host(p), want) == -1
 
 
+# Chunk lengths K around the 16-coefficient groups of the evaluation's and the
+# division's dot products (one group, one group and one term, two groups, ...):
+# n = SMs x blocks per SM x 256 x K gives exactly K per thread (evaluation: 1
+# block per SM up to 2^21 coefficients, 2 above; division: 2).
+@pytest.mark.parametrize("k", [15, 16, 17, 31, 32, 33])
+def test_eval_div_group_boundaries(pp, O, cuda, k):
+    sms = cuda.cuda.get_device_properties(0).multi_processor_count
+    for op, bps in (("eval", 1), ("div", 2)):
+        n = sms * bps * 256 * k
+        if op == "eval" and n > (1 << 21):
+            n = sms * 2 * 256 * k
+        p = pp.random_fr(n, 800 + k)
+        c = pp.random_fr(1, 801 + k)
+        if op == "eval":
+            assert (host(pp.evaluate(p, c))[0] == O.evaluate(host(p), host(c)[0])).all(), (op, k, n)
+        else:
+            want = O.div_xplusc(host(p), host(c)[0])
+            pp.div_xplusc_(p, c)
+            assert O.first_diff(host(p), want) == -1, (op, k, n)
+
+
 def test_reference_cpu_goldens(pp, O, cuda, golden):
     """GPU results vs the reference's naive_gp / naive_div outputs, using the
     conventions of its GPU operators (exclusive product; quotient of length n
