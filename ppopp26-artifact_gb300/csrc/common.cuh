@@ -65,6 +65,8 @@ __device__ __forceinline__ void st_fr(fr *p, const fr &v) {
 void *workspace_get(size_t bytes, cudaStream_t stream, int slot, int *status);
 // frees every workspace of `stream` (call before destroying the stream)
 void workspace_release_stream(cudaStream_t stream);
+// destroys pp_ntt_host_many's cached copy streams and events (pp_release)
+void host_many_release();
 
 // counts kernel launches issued by this library (pp_launch_count)
 void count_launch();

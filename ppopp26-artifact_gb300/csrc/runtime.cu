@@ -117,6 +117,7 @@ int release_all() {
     g_ws.clear();
   }
   ntt_release_tables();
+  host_many_release();
   return PP_OK;
 }
 

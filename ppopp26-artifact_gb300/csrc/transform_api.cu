@@ -333,6 +333,33 @@ int host_many_ctx(cudaStream_t s, HostManyCtx **out) {
 }
 }  // namespace
 
+namespace pp {
+void host_many_release() {
+  std::lock_guard<std::mutex> lk(g_many_mu);
+  for (auto &kv : g_many) {
+    HostManyCtx *c = kv.second;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(kv.first.first);
+    cudaStreamSynchronize(c->s_in);
+    cudaStreamSynchronize(c->s_out);
+    cudaStreamDestroy(c->s_in);
+    cudaStreamDestroy(c->s_out);
+    cudaEventDestroy(c->ev_start);
+    cudaEventDestroy(c->ev_done);
+    for (int b = 0; b < 3; ++b) {
+      cudaEventDestroy(c->ev_in[b]);
+      cudaEventDestroy(c->ev_cmp[b]);
+      cudaEventDestroy(c->ev_out[b]);
+    }
+    cudaSetDevice(cur);
+    delete c;
+  }
+  g_many.clear();
+  cudaGetLastError();
+}
+}  // namespace pp
+
 extern "C" int pp_ntt_host_many(const void *const *h_in, void *const *h_out, uint32_t count,
                                 uint32_t lg_n, int inverse, void *stream) {
   if (lg_n > PP_MAX_LG_N) {
