@@ -34,6 +34,13 @@ namespace pp {
 // latency).  Evaluation has its own geometry (k_eval_tree).
 constexpr uint32_t kGpBlocksPerSm = 2, kDivBlocksPerSm = 2,
                    kPermBlocksPerSm = 8;
+// The grand product's chains grow with n while its block trees do not: at
+// 2^22 3 blocks per SM beat 2 (0.210 against 0.220 ms), at 2^24 4 beat 2 and 3
+// (0.712 against 0.764 / 0.730 ms); at 2^20 2 stays best (4: 0.081 against
+// 0.075 ms).  The division's replay was best at 2 for all three sizes.
+inline uint32_t gp_blocks_per_sm(uint64_t n) {
+  return n <= (1ull << 21) ? kGpBlocksPerSm : n <= (1ull << 23) ? 3 : 4;
+}
 
 // ---------------------------------------------------------------- helpers
 // Block scans are work-efficient (Blelloch, "Prefix sums and their
@@ -754,7 +761,7 @@ extern "C" int pp_gp_scan(const void *d_in, void *d_excl, void *d_incl, uint64_t
     return PP_E_INVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const pp::ScanGeom g = pp::scan_geom(n, pp::kGpBlocksPerSm);
+  const pp::ScanGeom g = pp::scan_geom(n, pp::gp_blocks_per_sm(n));
   int st = PP_OK;
   fr *ws = static_cast<fr *>(
       pp::workspace_get((g.threads + g.blocks) * sizeof(fr), s, 1, &st));

@@ -21,6 +21,15 @@ def test_gp_prefix(pp, O, cuda, n):
     assert O.first_diff(host(x), want) == -1
 
 
+@pytest.mark.parametrize("n", [(1 << 22) + 3, 1 << 24])
+def test_gp_prefix_large(pp, O, cuda, n):
+    """The sizes that run 3 and 4 blocks per SM."""
+    x = pp.random_fr(n, 550 + n % 1000)
+    want = O.gp_prefix(host(x))
+    pp.gp_prefix_(x)
+    assert O.first_diff(host(x), want) == -1
+
+
 @pytest.mark.parametrize("n", SIZES)
 def test_eval(pp, O, cuda, n):
     p = pp.random_fr(n, 600 + n)
