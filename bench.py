@@ -145,20 +145,22 @@ def profile_traffic(name: str):
 
 
 def measure_int_rates(ppfr):
-    """Measured integer-pipe rates of this GPU (pp_measure_int_rates), the
+    """Measured integer-pipe rates of this GPU (pp_measure_int_rates_ex), the
     denominators of the integer roofline: lane operations per second of
-    mad.lo.u32 / mad.hi.u32 / mad.wide.u32 loops at full occupancy, and the
-    standalone Montgomery multiply rate."""
+    mad.lo.u32 / mad.hi.u32 / mad.wide.u32 loops at full occupancy, the
+    standalone Montgomery multiply rate, and the wide product without its
+    64-bit addend (alone, and with the addend as a separate add.u64)."""
     import ctypes
 
     L = ppfr.lib()
-    f = L.pp_measure_int_rates
-    f.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    f = L.pp_measure_int_rates_ex
+    f.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
     f.restype = ctypes.c_int
-    out = (ctypes.c_double * 4)()
-    ppfr.check(f(out))
+    out = (ctypes.c_double * 6)()
+    ppfr.check(f(out, 6))
     return {"mad_lo_per_s": out[0], "mad_hi_per_s": out[1], "mad_wide_per_s": out[2],
-            "mont_mul_per_s": out[3]}
+            "mont_mul_per_s": out[3], "mul_wide_no_addend_per_s": out[4],
+            "mul_wide_then_add_u64_per_s": out[5]}
 
 
 def reduce_max_over_ranks(values, dist, device):

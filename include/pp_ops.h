@@ -73,8 +73,14 @@ int pp_tune_load(const char *path);
  * integer roofline: out[0] mad.lo.u32, out[1] mad.hi.u32, out[2] mad.wide.u32
  * (64-bit addend) lane operations per second, each from a full-occupancy loop
  * of independent chains; out[3] standalone Montgomery multiplies per second.
- * No counterpart in the reference.  About 30 ms of GPU time. */
+ * No counterpart in the reference.  About 40 ms of GPU time. */
 int pp_measure_int_rates(double out[4]);
+
+/* The same rates and two more: out[4] mul.wide.u32 (no addend) lane
+ * operations per second, out[5] mul.wide.u32 followed by a dependent add.u64
+ * (the addend on the ALU instead), per second.  n is 4 .. 6; out[i] for
+ * i < n is written.  No counterpart in the reference. */
+int pp_measure_int_rates_ex(double *out, int n);
 
 /* ---------------------------------------------------------------- LDE ---
  * Low-degree extension onto 2^(lg_n+lambda) points, natural order out.

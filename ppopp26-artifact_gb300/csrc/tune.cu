@@ -234,12 +234,21 @@ __global__ void __launch_bounds__(256) k_int_rate(uint32_t seed, uint32_t *sink)
         asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(acc[k]) : "r"(a), "r"(b));
       } else if (KIND == 1) {
         asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(acc[k]) : "r"(a), "r"(b));
-      } else {
+      } else if (KIND == 2) {
         // 32 x 32 -> 64-bit product with a 64-bit addend: the row product of
         // the Montgomery multiply
         // the multiplicand is the accumulator's low word, so the product
         // depends on the chain and cannot be hoisted out of the loop
         asm volatile("{\n\t.reg .u32 l, h;\n\tmov.b64 {l, h}, %0;\n\tmad.wide.u32 %0, l, %1, %0;\n\t}"
+                     : "+l"(wide[k]) : "r"(a));
+      } else if (KIND == 3) {
+        // the same product without the addend
+        asm volatile("{\n\t.reg .u32 l, h;\n\tmov.b64 {l, h}, %0;\n\tmul.wide.u32 %0, l, %1;\n\t}"
+                     : "+l"(wide[k]) : "r"(a));
+      } else {
+        // the product without the addend, then the addend as a 64-bit add
+        asm volatile("{\n\t.reg .u32 l, h;\n\t.reg .u64 p;\n\tmov.b64 {l, h}, %0;\n\t"
+                     "mul.wide.u32 p, l, %1;\n\tadd.u64 %0, %0, p;\n\t}"
                      : "+l"(wide[k]) : "r"(a));
       }
     }
@@ -274,10 +283,20 @@ __global__ void __launch_bounds__(256) k_mm_rate(const fr *in, fr *sink, int ite
 
 // out[0]: mad.lo.u32, out[1]: mad.hi.u32, out[2]: mad.wide.u32 lane operations
 // per second; out[3]: Montgomery multiplies per second (two independent chains
-// per thread, the standalone rate of the field multiply).  Uses a 1 KiB
-// workspace; about 30 ms of GPU time.
+// per thread, the standalone rate of the field multiply); out[4]: mul.wide.u32
+// (no addend) lane operations per second; out[5]: mul.wide.u32 followed by a
+// dependent add.u64, per second.  Uses a 1 KiB workspace; about 40 ms of GPU
+// time.
 extern "C" int pp_measure_int_rates(double out[4]) {
-  if (!out) return PP_E_INVAL;
+  double all[6];
+  const int st = pp_measure_int_rates_ex(all, 6);
+  if (st == PP_OK)
+    for (int i = 0; i < 4; ++i) out[i] = all[i];
+  return st;
+}
+
+extern "C" int pp_measure_int_rates_ex(double *out, int n) {
+  if (!out || n < 4 || n > 6) return PP_E_INVAL;
   int dev = 0;
   PP_CUDA_TRY(cudaGetDevice(&dev));
   const int sms = pp::device_sm_count();
@@ -289,19 +308,24 @@ extern "C" int pp_measure_int_rates(double out[4]) {
   PP_CUDA_TRY(cudaEventCreate(&e0));
   PP_CUDA_TRY(cudaEventCreate(&e1));
   const double lane_ops = (double)blocks * 256 * pp::kIntIters * pp::kIntChains;
-  for (int kind = 0; kind < 3 && st == PP_OK; ++kind) {
+  static const int kKindSlot[5] = {0, 1, 2, 4, 5};
+  for (int kind = 0; kind < 5 && st == PP_OK; ++kind) {
+    const int slot = kKindSlot[kind];
+    if (slot >= n) continue;
     float ms = 0;
     for (int rep = 0; rep < 2; ++rep) {  // the first launch warms up
       cudaEventRecord(e0, nullptr);
       if (kind == 0) pp::k_int_rate<0><<<blocks, 256>>>(0x1234u + rep, ws);
       else if (kind == 1) pp::k_int_rate<1><<<blocks, 256>>>(0x1234u + rep, ws);
-      else pp::k_int_rate<2><<<blocks, 256>>>(0x1234u + rep, ws);
+      else if (kind == 2) pp::k_int_rate<2><<<blocks, 256>>>(0x1234u + rep, ws);
+      else if (kind == 3) pp::k_int_rate<3><<<blocks, 256>>>(0x1234u + rep, ws);
+      else pp::k_int_rate<4><<<blocks, 256>>>(0x1234u + rep, ws);
       PP_COUNT_LAUNCH();
       cudaEventRecord(e1, nullptr);
       if (cudaEventSynchronize(e1) != cudaSuccess) st = PP_E_CUDA;
       cudaEventElapsedTime(&ms, e0, e1);
     }
-    out[kind] = lane_ops / (ms * 1e-3);
+    out[slot] = lane_ops / (ms * 1e-3);
   }
   if (st == PP_OK) {
     // field-multiply rate: inputs are 17 small Montgomery values
