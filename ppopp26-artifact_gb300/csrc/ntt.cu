@@ -141,7 +141,11 @@ __device__ __forceinline__ fr split_layer_twiddle(const PassArgs &a, uint32_t o,
 // One tile of one pass.  The block may be wider than the tile needs (batched
 // launches use 256 threads for every job); surplus threads only join the
 // barriers.
+template <bool HOSTIO>
 __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tileid, uint4 *sm) {
+  // HOSTIO = false compiles out the host-endpoint paths (unit_in, unit_out);
+  // every pass is still correct without them, with element-wise accesses
+  const bool unit_in = HOSTIO && a.unit_in, unit_out = HOSTIO && a.unit_out;
   const SmemTile tile{sm, a.lgT};
   const uint32_t R = 1u << a.lgR, T = 1u << a.lgT, E = R << a.lgT;
   const uint32_t nthr = E >> 3;
@@ -174,36 +178,51 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
 
   // ---- load the tile (coalesced) into shared memory.  A host-memory input
   // without a multiply on the way in moves 16-byte halves, so one warp
-  // instruction reads whole 128-byte lines.
-  if (a.unit_in && !(a.first && a.in_kind == NTT_IN_DIAG)) {
+  // instruction reads whole 128-byte lines; a thread's 16 loads issue in two
+  // groups of eight before their shared-memory stores, so it waits on host
+  // memory twice per tile instead of sixteen times.
+  auto tile_src = [&](uint32_t e, uint32_t &n, uint32_t &col) -> uint64_t {
+    if (!a.last) {
+      n = e >> a.lgT;
+      col = e & (T - 1);
+      return base + ((uint64_t)n << a.lgS) + col;
+    }
+    if (a.P == 1) {
+      n = e;
+      col = 0;
+      return n;
+    }
+    n = e & (R - 1);
+    col = e >> a.lgR;
+    return in_base + ((uint64_t)col << lgS1) + n;
+  };
+  if (unit_in && !(a.first && a.in_kind == NTT_IN_DIAG)) {
     const uint4 zero4 = make_uint4(0, 0, 0, 0);
-    for (uint32_t u = tid; active && u < 2 * E; u += nthr) {
-      const uint32_t e = u >> 1, h = u & 1;
-      uint32_t n, col;
-      uint64_t g;
-      if (!a.last) {
-        n = e >> a.lgT;
-        col = e & (T - 1);
-        g = base + ((uint64_t)n << a.lgS) + col;
-      } else if (a.P == 1) {
-        n = e;
-        col = 0;
-        g = n;
-      } else {
-        n = e & (R - 1);
-        col = e >> a.lgR;
-        g = in_base + ((uint64_t)col << lgS1) + n;
+    if (active) {
+#pragma unroll
+      for (uint32_t k0 = 0; k0 < 16; k0 += 8) {
+        uint4 v[8];
+        uint32_t dst[8];
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) {
+          const uint32_t u = tid + (k0 + i) * nthr;
+          const uint32_t e = u >> 1, h = u & 1;
+          uint32_t n, col;
+          const uint64_t g = tile_src(e, n, col);
+          dst[i] = swz((((n << a.lgT) + col) << 1) + h);
+          v[i] = zero4;
+          if (!a.first) {
+            v[i] = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
+          } else if (a.in_kind == NTT_IN_SPREAD) {
+            if ((g & ((1ull << a.spread) - 1)) == 0)
+              v[i] = __ldcs(reinterpret_cast<const uint4 *>(a.in + (g >> a.spread)) + h);
+          } else if (g < a.n_valid) {
+            v[i] = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
+          }
+        }
+#pragma unroll
+        for (uint32_t i = 0; i < 8; ++i) tile.s[dst[i]] = v[i];
       }
-      uint4 v = zero4;
-      if (!a.first) {
-        v = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
-      } else if (a.in_kind == NTT_IN_SPREAD) {
-        if ((g & ((1ull << a.spread) - 1)) == 0)
-          v = __ldcs(reinterpret_cast<const uint4 *>(a.in + (g >> a.spread)) + h);
-      } else if (g < a.n_valid) {
-        v = __ldcs(reinterpret_cast<const uint4 *>(a.in + g) + h);
-      }
-      tile.s[swz((((n << a.lgT) + col) << 1) + h)] = v;
     }
   } else {
     for (uint32_t e = tid; active && e < E; e += nthr) {
@@ -293,7 +312,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
             const uint32_t k = ((i & 1) << 2) | (i & 2) | ((i >> 2) & 1);
             x[i] = fr_mul_twiddle(x[i], ldg_fr(a.tw_inner + ((c * k) << lgP)));
           }
-        } else if (a.last && a.unit_out) {
+        } else if (a.last && unit_out) {
           // the 16-byte store path copies tile words: canonical here
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
@@ -325,7 +344,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
 #pragma unroll
           for (int h = 0; h < 8; h += 2) bfly(x[h], x[h + 1]);
         }
-        if (a.last && a.unit_out) {
+        if (a.last && unit_out) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = fr_canon(x[i]);
         }
@@ -341,7 +360,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
   // ---- store (coalesced), with the layer twiddle or the final scale.  A
   // host-memory output without a scale moves 16-byte halves, so one warp
   // instruction writes whole 128-byte lines (partial lines cost C2C bandwidth).
-  if (a.last && a.unit_out && !a.has_post_scale) {
+  if (a.last && unit_out && !a.has_post_scale) {
     for (uint32_t u = tid; active && u < 2 * E; u += nthr) {
       const uint32_t e = u >> 1, h = u & 1;
       uint32_t o, col;
@@ -359,7 +378,7 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
     }
     return;
   }
-  if (!a.last && a.unit_out) {
+  if (!a.last && unit_out) {
     // host output of an intermediate pass: the layer twiddles go into the
     // tile first, then whole 128-byte lines leave it
     if (a.tw_layer || a.tw_lo) {
@@ -406,9 +425,10 @@ __device__ __forceinline__ void ntt_tile(const PassArgs &a, const uint64_t tilei
 #ifndef PP_NTT_MINB
 #define PP_NTT_MINB 2  // blocks per SM the pass kernels are compiled for
 #endif
+template <bool HOSTIO>
 __global__ void __launch_bounds__(256, PP_NTT_MINB) k_ntt_pass(const PassArgs a) {
   extern __shared__ uint4 sm[];
-  ntt_tile(a, blockIdx.x, sm);
+  ntt_tile<HOSTIO>(a, blockIdx.x, sm);
 }
 
 // One batch level: the tiles of every job pass at this level are numbered
@@ -423,7 +443,7 @@ __global__ void __launch_bounds__(256, PP_NTT_MINB) k_ntt_batch_level(const __gr
     if (p.tile_start[mid] <= t) lo = mid;
     else hi = mid;
   }
-  ntt_tile(p.args[lo], t - p.tile_start[lo], sm);
+  ntt_tile<false>(p.args[lo], t - p.tile_start[lo], sm);  // device endpoints
 }
 
 // Transforms of 2^3 .. 2^11 points (single-pass plans) in one block: the
@@ -923,7 +943,9 @@ int describe_passes(const fr *d_in, fr *d_out, fr *work, uint32_t lg_m, bool inv
     int st = get_plan(dev, lg_m, inverse, &plan, small, split);
     if (st) return st;
     if (dev < 64 && !g_attr_set[dev]) {
-      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2048 * (int)sizeof(fr)));
+      PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        2048 * (int)sizeof(fr)));
       PP_CUDA_TRY(cudaFuncSetAttribute(k_ntt_batch_level,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1043,7 +1065,10 @@ int ntt_run(const fr *d_in, fr *d_out, uint32_t lg_m, bool inverse, const NttInp
   }
   for (size_t j = 0; j < passes.size(); ++j) {
     const uint32_t E = 1u << (passes[j].lgR + passes[j].lgT);
-    k_ntt_pass<<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(passes[j]);
+    if (passes[j].unit_in || passes[j].unit_out)
+      k_ntt_pass<true><<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(passes[j]);
+    else
+      k_ntt_pass<false><<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(passes[j]);
     PP_COUNT_LAUNCH();
     PP_LAUNCH_CHECK();
   }
@@ -1109,7 +1134,7 @@ int ntt_run_host_passes(const fr *h_in, fr *h_out, fr *h_scratch, uint32_t lg_m,
     a.unit_in = 1;
     a.unit_out = 1;
     const uint32_t E = 1u << (a.lgR + a.lgT);
-    k_ntt_pass<<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(a);
+    k_ntt_pass<true><<<(unsigned)tiles[j], E / 8, E * sizeof(fr), stream>>>(a);
     PP_COUNT_LAUNCH();
     PP_LAUNCH_CHECK();
   }
