@@ -40,3 +40,9 @@ def test_invalid_arguments_are_reported_not_fatal(pp):
     assert b"aligned" in L.pp_last_error()
     assert L.pp_lde(ctypes.c_void_p(16), ctypes.c_void_p(32), 10, 9, 0, None) == 1  # lambda > 8
     assert L.pp_ntt(ctypes.c_void_p(16), ctypes.c_void_p(16), 31, 0, None) == 5  # unsupported size
+    # the integer-rate probe checks its output array before any launch
+    L.pp_measure_int_rates_ex.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    out = (ctypes.c_double * 6)()
+    assert L.pp_measure_int_rates_ex(None, 6) == 1
+    assert L.pp_measure_int_rates_ex(out, 3) == 1
+    assert L.pp_measure_int_rates_ex(out, 7) == 1
