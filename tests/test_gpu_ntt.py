@@ -110,9 +110,9 @@ def test_lde_modes_bit_exact(pp, O, cuda, lg, lam):
 
 @pytest.mark.parametrize("lg,lam", [(22, 2), (22, 3), (24, 2), (24, 3)])
 def test_lde_benchmark_sizes_bit_exact(pp, O, cuda, lg, lam):
-    """The benchmark LDE sizes in both coset forms, every one of the
+    """The benchmark LDE sizes in all three forms, every one of the
     2^(lg+lam) outputs against the oracle: from coefficients (shift
-    7^(2^lam)) and from evaluations (INTT, then shift 7)."""
+    7^(2^lam)), from evaluations (INTT, then shift 7) and spread."""
     x = pp.random_fr(1 << lg, 0x1DE0 + 16 * lg + lam)
     xh = host(x)
     out = host(pp.lde(x, lam, pp.LDE_COEFFS))
@@ -120,3 +120,8 @@ def test_lde_benchmark_sizes_bit_exact(pp, O, cuda, lg, lam):
     del out
     out = host(pp.lde(x, lam, pp.LDE_EVALS))
     assert O.first_diff(out, O.lde_evals(xh, lam)) == -1
+    del out
+    # the spread form (the reference's naive_lde input layout): the oracle runs
+    # the whole 2^(lg+lam)-point transform of the zero-spread input
+    out = host(pp.lde(x, lam, pp.LDE_SPREAD))
+    assert O.first_diff(out, O.lde_spread(xh, lam)) == -1
